@@ -1,0 +1,437 @@
+"""Benchmark: vgh spline-evaluations/s of a uniform 3D multi-spline, 64^3 grid,
+1024 real orbitals, FP16 coefficient table vs FP32, with request latency.
+
+A step is one vgh pass over one batch of 64 walkers whose point counts are
+uniform in {32..512} (about 17.6k points, positions uniform in the unit box),
+every (point, spline) pair producing value, gradient and Hessian.  Each step
+uses a different batch of points; the tables (1.23 GB FP32, 0.62 GB FP16) and
+the stencil rows a batch touches are far larger than the 126 MB L2.
+
+Prints one JSON line (rank 0).  `--impl reference` times the reference's CPU
+path instead (the oracle's port of eval_multi_UBspline_3d_s_vgh, OpenMP over
+points on all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID = 64
+NSPL = 1024
+WALKERS = 64
+SEED_DATA = 20261203
+SEED_PTS = 777
+METRIC = "vgh spline-evals/s (64³, 1024 orbitals) FP16-coef vs FP32; p50/p99 latency"
+UNIT = "spline-evals/s"
+BYTES_F32 = 64 * 4 + 10 * 4   # algorithmic bytes per vgh spline-eval, FP32 table
+BYTES_F16 = 64 * 2 + 10 * 4   # FP16 table (per-spline scale amortised to 0)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(key):
+    """DRAM bytes per spline-eval from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during a timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.th = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.th:
+                self.th.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+            except Exception:
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_batches(nbatches, seed):
+    """nbatches walker batches: (points [P,3] float64, walker sizes)."""
+    from einspline_gb300 import synth
+    out = []
+    for b in range(nbatches):
+        sizes = synth.walker_sizes(seed + 2 * b, WALKERS)
+        pts = synth.points_uniform(seed + 2 * b + 1, int(sizes.sum()))
+        out.append((pts, sizes))
+    return out
+
+
+def build_tables(device_data=True):
+    import torch
+    from einspline_gb300 import api
+    grids = [(0.0, 1.0, GRID)] * 3
+    bcs = [(api.PERIODIC, api.PERIODIC)] * 3
+    per = GRID ** 3
+    tabs = {}
+    for name, st in (("f32", api.STORE_F32), ("f16", api.STORE_F16)):
+        tabs[name] = api.MultiUBspline3D("s", grids, bcs, NSPL, storage=st)
+    chunk = 128
+    buf = torch.empty((chunk, GRID, GRID, GRID), dtype=torch.float32, device="cuda")
+    for first in range(0, NSPL, chunk):
+        # same splitmix64 stream as synth.grid_data_uniform(SEED_DATA, ...)
+        api.fill_uniform(buf, SEED_DATA, -1.0, 1.0, offset=first * per)
+        for t in tabs.values():
+            t.set_device(first, buf)
+    for t in tabs.values():
+        t.flush()
+    torch.cuda.synchronize()
+    return tabs
+
+
+def cpu_eval_rate(table_f32: np.ndarray, ncol_pad: int, seconds: float, nthreads: int = 0):
+    """The oracle's port of the reference CPU vgh evaluation (OpenMP over
+    points), on the FP32 table, for about `seconds`.  Returns evals/s, cores,
+    sample description."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    L = O.lib(fast=True)
+    desc = O.OrcDesc()
+    for a in range(3):
+        L.orc_axis_init(C.byref(desc.ax[a]), 0.0, 1.0, GRID, O.PERIODIC, O.PERIODIC, 0, 0, 0, 0)
+    desc.num_splines = NSPL
+    desc.zs = ncol_pad
+    desc.ys = (GRID + 3) * ncol_pad
+    desc.xs = (GRID + 3) * desc.ys
+    cores = nthreads if nthreads > 0 else L.orc_max_threads()
+    from einspline_gb300 import synth
+    npts = 4 * cores
+    v = np.empty((npts, NSPL), np.float32)
+    g = np.empty((npts, NSPL, 3), np.float32)
+    h = np.empty((npts, NSPL, 3, 3), np.float32)
+    done, it = 0, 0
+    t0 = time.perf_counter()
+    while True:
+        pos = synth.points_uniform(99 + it, npts)
+        L.orc_eval_batch(ord("s"), 0, 1, C.byref(desc), C.c_void_p(table_f32.ctypes.data), npts,
+                         C.c_void_p(pos.ctypes.data), C.c_void_p(v.ctypes.data), C.c_void_p(g.ctypes.data),
+                         C.c_void_p(h.ctypes.data), cores)
+        done += npts
+        it += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    rate = done * NSPL / el
+    sample = f"{done} points x {NSPL} splines vgh (FP32 table 64^3), {el:.1f} s"
+    return rate, cores, sample
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from concurrent.futures import ThreadPoolExecutor
+    from einspline_gb300 import synth
+    O.build()
+    # Table built by the oracle's FP64 solve on the host (not timed).
+    grids = [(0.0, 1.0, GRID)] * 3
+    T = O.Table("s", grids, [(O.PERIODIC, O.PERIODIC)] * 3, NSPL)
+    per = GRID ** 3
+
+    def one(i):
+        d = synth.uniform(SEED_DATA, per, -1.0, 1.0, offset=i * per).astype(np.float32).astype(np.float64)
+        O.lib().orc_set_3d_column_d(C.byref(T.desc), 1, i, O.ptr(T.coefs64), O.ptr(d.reshape(GRID, GRID, GRID)))
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+        list(ex.map(one, range(NSPL)))
+    table = np.ascontiguousarray(T.coefs64.astype(np.float32))
+    del T
+    rates = []
+    per_step = max(2.0, 20.0 / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_eval_rate(table, NSPL, 0.5)
+    for _ in range(args.steps):
+        r, cores, sample = cpu_eval_rate(table, NSPL, per_step)
+        rates.append(r)
+    val = statistics.median(rates)
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample + f"; median of {args.steps} steps"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config():
+    return {"workload": "multi_UBspline_3d_s periodic 64^3 grid, 1024 real splines, vgh; step = 64 walkers x "
+                        "U{32..512} points uniform in the unit box (distinct points every step; tables and "
+                        "touched rows >> 126 MB L2, no flush needed)",
+            "grid": [GRID, GRID, GRID], "num_splines": NSPL, "walkers_per_step": WALKERS,
+            "points_per_walker": [32, 512], "tables": {"f32_bytes": 67 ** 3 * NSPL * 4, "f16_bytes": 67 ** 3 * NSPL * 2},
+            "l2": "inputs larger than L2"}
+
+
+def run_gpu(args):
+    import torch
+    from einspline_gb300 import api
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    tabs = build_tables()
+    nb = args.warmup + args.steps
+    batches = make_batches(nb, SEED_PTS + 1000 * rank)
+    maxp = max(p.shape[0] for p, _ in batches)
+    pos_d = [torch.from_numpy(p).cuda() for p, _ in batches]
+    npts = [p.shape[0] for p, _ in batches]
+    out = (torch.empty((maxp, NSPL), device="cuda"), torch.empty((maxp, NSPL, 3), device="cuda"),
+           torch.empty((maxp, NSPL, 6), device="cuda"))
+    stream = torch.cuda.current_stream()
+
+    def tune(t):
+        if args.autotune:
+            t.autotune(int(np.mean(npts)), True)
+
+    for t in tabs.values():
+        tune(t)
+
+    def timed(t):
+        for k in range(args.warmup):
+            P = npts[k]
+            t.eval(pos_d[k], vgh=True, rule=0, layout=0, out=(out[0][:P], out[1][:P], out[2][:P]))
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        n0 = api.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        evals = 0
+        for k in range(args.warmup, nb):
+            P = npts[k]
+            t.eval(pos_d[k], vgh=True, rule=0, layout=0, out=(out[0][:P], out[1][:P], out[2][:P]))
+            evals += P * NSPL
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ms = e0.elapsed_time(e1)
+        launches = api.launch_count() - n0
+        if dist:
+            tt = torch.tensor([ms], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            ms = float(tt.item())
+            ev = torch.tensor([float(evals)], device="cuda")
+            dist.all_reduce(ev)
+            evals = float(ev.item())
+        return evals, ms, launches
+
+    with ClockSampler(local) as clk:
+        ev16, ms16, l16 = timed(tabs["f16"])
+        ev32, ms32, l32 = timed(tabs["f32"])
+        # repeat the headline loop once more so the sampler sees sustained load
+        ev16b, ms16b, _ = timed(tabs["f16"])
+    ms16 = min(ms16, ms16b) if args.steps > 0 else ms16
+    rate16 = ev16 / (ms16 / 1e3)
+    rate32 = ev32 / (ms32 / 1e3)
+    per_launch_ms = ms16 / args.steps
+    evals_per_launch = ev16 / args.steps / world
+    peak, peak_kind = measured_peak()
+    achieved = evals_per_launch * BYTES_F16 / (per_launch_ms / 1e3) / 1e9
+    tr = profile_traffic("f16_vgh_bytes_per_eval")
+
+    # end to end through the host-buffer C-ABI entry: pinned positions in,
+    # pinned results out, copies inside the timed region
+    e2e = None
+    if args.e2e_steps > 0:
+        t = tabs["f16"]
+        hp = [torch.from_numpy(p).pin_memory() for p, _ in batches[:max(1, args.e2e_steps)]]
+        ho = (torch.empty((maxp, NSPL), pin_memory=True), torch.empty((maxp, NSPL, 3), pin_memory=True),
+              torch.empty((maxp, NSPL, 6), pin_memory=True))
+        for k in range(min(2, len(hp))):
+            P = hp[k].shape[0]
+            t.eval_host(hp[k].numpy(), out=(ho[0][:P].numpy(), ho[1][:P].numpy(), ho[2][:P].numpy()))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev, h2d, d2h = 0, 0, 0
+        for k in range(len(hp)):
+            P = hp[k].shape[0]
+            t.eval_host(hp[k].numpy(), out=(ho[0][:P].numpy(), ho[1][:P].numpy(), ho[2][:P].numpy()))
+            ev += P * NSPL
+            h2d += P * 24
+            d2h += P * NSPL * 10 * 4
+        el = time.perf_counter() - t0
+        e2e = {"value": ev / el * world, "unit": UNIT, "h2d_bytes_per_step": h2d // len(hp),
+               "d2h_bytes_per_step": d2h // len(hp), "path": "einspline_gb300_eval_3d_host (pinned host buffers)"}
+
+    # request latency: each walker evaluated alone, arrival-to-ready on the device
+    lat = []
+    if args.latency_requests > 0:
+        t = tabs["f16"]
+        from einspline_gb300 import synth
+        sizes = synth.walker_sizes(4242, args.latency_requests)
+        for i, n in enumerate(sizes):
+            p = torch.from_numpy(synth.points_uniform(5000 + i, int(n))).cuda()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            t.eval(p, vgh=True, rule=0, layout=0, out=(out[0][:n], out[1][:n], out[2][:n]))
+            torch.cuda.synchronize()
+            lat.append((time.perf_counter() - t0) * 1e3)
+
+    cpu = None
+    if rank == 0 and args.cpu_seconds > 0:
+        raw, _ = tabs["f32"].table_host()
+        cpu_rate, cores, sample = cpu_eval_rate(np.ascontiguousarray(raw), raw.shape[-1], args.cpu_seconds)
+        cpu = {"value": cpu_rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    err = None
+    if rank == 0 and args.error_points > 0:
+        err = precision_report(tabs, args.error_points)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": rate16, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms16 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16-table/f32-math", "data": "synthetic",
+        "config": workload_config(),
+        "fp32_table": {"value": rate32, "ms_per_step": ms32 / args.steps, "launches": l32},
+        "fp16_vs_fp32": rate16 / rate32,
+        "latency_ms": ({"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                        "requests": len(lat), "mode": "one walker per launch, host clock, device idle otherwise"}
+                       if lat else None),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "k_eval<F16,vgh>",
+                     "bytes_per_eval": BYTES_F16,
+                     "traffic": (tr * evals_per_launch if tr else None),
+                     "fp32": {"achieved": rate32 / world * BYTES_F32 / 1e9,
+                              "frac": rate32 / world * BYTES_F32 / 1e9 / peak}},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": l16,
+        "clocks": clk.summary(),
+        "error_vs_fp64": err,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def precision_report(tabs, npts):
+    """Max and RMS error of value, gradient and Hessian of both tables against
+    the FP64 oracle on sampled spline columns (relative to each quantity's
+    max magnitude)."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from einspline_gb300 import synth
+    cols = list(range(0, NSPL, NSPL // 16))
+    grids = [(0.0, 1.0, GRID)] * 3
+    T = O.Table("d", grids, [(O.PERIODIC, O.PERIODIC)] * 3, len(cols))
+    per = GRID ** 3
+    for j, c in enumerate(cols):
+        d = synth.uniform(SEED_DATA, per, -1.0, 1.0, offset=c * per).astype(np.float32).astype(np.float64)
+        T.set_spline(j, d.reshape(GRID, GRID, GRID))
+    pos = synth.points_uniform(31337, npts)
+    rv, rg, rh = T.eval(pos, vgh=True, sem=0)
+    rh = rh.reshape(npts, len(cols), 9)[:, :, [0, 1, 2, 4, 5, 8]]
+    rep = {}
+    for name, t in tabs.items():
+        v, g, h = (x.cpu().numpy() for x in t.eval(torch.from_numpy(pos).cuda(), vgh=True, rule=0, layout=0))
+        q = {}
+        for qn, a, b in (("value", v[:, cols], rv), ("gradient", g[:, cols], rg), ("hessian", h[:, cols], rh)):
+            d = (a.astype(np.float64) - b) / np.abs(b).max()
+            q[qn] = {"max": float(np.abs(d).max()), "rms": float(np.sqrt((d ** 2).mean()))}
+        rep[name] = q
+    rep["note"] = (f"{npts} points x {len(cols)} sampled splines vs eval_multi_UBspline_3d_d on the FP64 table; "
+                   "errors relative to max |quantity|")
+    return rep
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--latency-requests", type=int, default=200)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--error-points", type=int, default=256)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

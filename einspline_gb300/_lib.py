@@ -1,0 +1,188 @@
+"""ctypes binding of the C-ABI library libeinspline_gb300.so.
+
+Structures mirror include/*.h field for field.  Loading fails loudly when the
+library has not been built: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+PERIODIC, DERIV1, DERIV2, FLAT, NATURAL, ANTIPERIODIC = range(6)
+SINGLE_REAL, DOUBLE_REAL, SINGLE_COMPLEX, DOUBLE_COMPLEX = range(4)
+STORE_NATIVE, STORE_F32, STORE_F16, STORE_BF16, STORE_F64 = range(5)
+STORAGE_NAMES = {STORE_NATIVE: "native", STORE_F32: "f32", STORE_F16: "f16", STORE_BF16: "bf16", STORE_F64: "f64"}
+
+
+class Ugrid(C.Structure):
+    _fields_ = [("start", C.c_double), ("end", C.c_double), ("num", C.c_int),
+                ("delta", C.c_double), ("delta_inv", C.c_double)]
+
+
+class BCtype_s(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal", C.c_float), ("rVal", C.c_float)]
+
+
+class BCtype_d(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal", C.c_double), ("rVal", C.c_double)]
+
+
+class BCtype_c(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal_r", C.c_float), ("lVal_i", C.c_float),
+                ("rVal_r", C.c_float), ("rVal_i", C.c_float)]
+
+
+class BCtype_z(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal_r", C.c_double), ("lVal_i", C.c_double),
+                ("rVal_r", C.c_double), ("rVal_i", C.c_double)]
+
+
+BC_TYPES = {"s": BCtype_s, "d": BCtype_d, "c": BCtype_c, "z": BCtype_z}
+
+
+def _host_struct(kind):
+    fields = [("spcode", C.c_int), ("tcode", C.c_int), ("coefs", C.c_void_p),
+              ("x_stride", C.c_ssize_t), ("y_stride", C.c_ssize_t), ("z_stride", C.c_ssize_t),
+              ("x_grid", Ugrid), ("y_grid", Ugrid), ("z_grid", Ugrid),
+              ("xBC", BC_TYPES[kind]), ("yBC", BC_TYPES[kind]), ("zBC", BC_TYPES[kind]),
+              ("num_splines", C.c_int)]
+    if kind in "cz":
+        fields.append(("lapl3", C.c_void_p))
+    fields.append(("gb300", C.c_void_p))
+    return type(f"multi_UBspline_3d_{kind}", (C.Structure,), {"_fields_": fields})
+
+
+HOST_STRUCTS = {k: _host_struct(k) for k in "sdcz"}
+
+
+class uint3(C.Structure):
+    _fields_ = [("x", C.c_uint), ("y", C.c_uint), ("z", C.c_uint)]
+
+
+class float3(C.Structure):
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("z", C.c_float)]
+
+
+class double3(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+def _cuda_struct(kind):
+    g = float3 if kind in "sc" else double3
+    fields = [("coefs", C.c_void_p), ("stride", uint3), ("gridInv", g), ("dim", uint3),
+              ("num_splines", C.c_int), ("gb300", C.c_void_p)]
+    return type(f"multi_UBspline_3d_{kind}_cuda", (C.Structure,), {"_fields_": fields})
+
+
+CUDA_STRUCTS = {k: _cuda_struct(k) for k in "sdcz"}
+
+
+class EvalOpts(C.Structure):
+    _fields_ = [("vgh", C.c_int), ("pos_f64", C.c_int), ("rule", C.c_int), ("layout", C.c_int),
+                ("sort", C.c_int), ("vstride", C.c_int64), ("gstride", C.c_int64), ("hstride", C.c_int64)]
+
+
+class TableInfo(C.Structure):
+    _fields_ = [("kind", C.c_int), ("storage", C.c_int), ("num_splines", C.c_int), ("ncol", C.c_int),
+                ("ncol_pad", C.c_int), ("elem_bytes", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+                ("nz", C.c_int), ("x_stride", C.c_int64), ("y_stride", C.c_int64), ("z_stride", C.c_int64),
+                ("table_bytes", C.c_uint64), ("coefs", C.c_void_p), ("scale", C.c_void_p)]
+
+
+# Every symbol the headers in include/ declare, with its ctypes signature.
+def _signatures():
+    vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
+    sig = {}
+    for k in "sdcz":
+        H = C.POINTER(HOST_STRUCTS[k])
+        D = C.POINTER(CUDA_STRUCTS[k])
+        BC = BC_TYPES[k]
+        sig[f"create_multi_UBspline_3d_{k}"] = ([Ugrid, Ugrid, Ugrid, BC, BC, BC, i32], H)
+        sig[f"set_multi_UBspline_3d_{k}"] = ([H, i32, vp], None)
+        sig[f"eval_multi_UBspline_3d_{k}"] = ([H, dbl, dbl, dbl, vp], None)
+        sig[f"eval_multi_UBspline_3d_{k}_vgh"] = ([H, dbl, dbl, dbl, vp, vp, vp], None)
+        sig[f"create_multi_UBspline_3d_{k}_cuda"] = ([H], D)
+        sig[f"destroy_multi_UBspline_3d_{k}_cuda"] = ([D], None)
+        sig[f"eval_multi_multi_UBspline_3d_{k}_cuda"] = ([D, vp, vp, i32], None)
+        sig[f"eval_multi_multi_UBspline_3d_{k}_vgh_cuda"] = ([D, vp, vp, vp, vp, i32], None)
+    sig["create_multi_UBspline_3d_s_cuda_conv"] = ([C.POINTER(HOST_STRUCTS["d"])], C.POINTER(CUDA_STRUCTS["s"]))
+    sig["create_multi_UBspline_3d_c_cuda_conv"] = ([C.POINTER(HOST_STRUCTS["z"])], C.POINTER(CUDA_STRUCTS["c"]))
+    sig["destroy_Bspline"] = ([vp], None)
+    sig["destroy_multi_UBspline"] = ([vp], None)
+    sig["einspline_gb300_create_3d_s"] = ([Ugrid, Ugrid, Ugrid, BCtype_s, BCtype_s, BCtype_s, i32, i32],
+                                          C.POINTER(HOST_STRUCTS["s"]))
+    sig["einspline_gb300_create_3d_c"] = ([Ugrid, Ugrid, Ugrid, BCtype_c, BCtype_c, BCtype_c, i32, i32],
+                                          C.POINTER(HOST_STRUCTS["c"]))
+    sig["einspline_gb300_create_3d_s_cuda_from_d"] = ([C.POINTER(HOST_STRUCTS["d"]), i32],
+                                                      C.POINTER(CUDA_STRUCTS["s"]))
+    sig["einspline_gb300_create_3d_c_cuda_from_z"] = ([C.POINTER(HOST_STRUCTS["z"]), i32],
+                                                      C.POINTER(CUDA_STRUCTS["c"]))
+    sig["einspline_gb300_last_error"] = ([], i32)
+    sig["einspline_gb300_last_error_message"] = ([], C.c_char_p)
+    sig["einspline_gb300_clear_error"] = ([], None)
+    sig["einspline_gb300_set_abort_on_error"] = ([i32], None)
+    sig["einspline_gb300_set_3d_device"] = ([vp, i32, i32, vp], i32)
+    sig["einspline_gb300_flush"] = ([vp], i32)
+    sig["einspline_gb300_get_table_info"] = ([vp, C.POINTER(TableInfo)], i32)
+    sig["einspline_gb300_copy_table"] = ([vp, vp, vp], i32)
+    sig["einspline_gb300_eval_3d"] = ([vp, C.POINTER(EvalOpts), i64, vp, vp, vp, vp, vp], i32)
+    sig["einspline_gb300_eval_3d_host"] = ([vp, C.POINTER(EvalOpts), i64, vp, vp, vp, vp], i32)
+    sig["einspline_gb300_set_tile"] = ([vp, i32, i32, i32], i32)
+    sig["einspline_gb300_get_tile"] = ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32)
+    sig["einspline_gb300_autotune"] = ([vp, i64, i32], i32)
+    sig["einspline_gb300_launch_count"] = ([], i64)
+    sig["einspline_gb300_fill_uniform"] = ([vp, i64, i32, C.c_uint64, i64, dbl, dbl, vp], i32)
+    return sig
+
+
+SIGNATURES = _signatures()
+# Library-internal helpers exported for tests (not part of include/).
+EXTRA_SIGNATURES = {
+    "einspline_gb300_solve_line_host": ([C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                         C.c_void_p, C.c_void_p], C.c_int),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Load the library (once).  Raises if it is missing: the product has no
+    CPU fallback."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            if build_if_missing:
+                _build.build()
+            else:
+                raise RuntimeError(f"einspline_gb300: {path} is missing; build it with "
+                                   "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(path)
+        for name, (args, res) in {**SIGNATURES, **EXTRA_SIGNATURES}.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        L.einspline_gb300_set_abort_on_error(0)
+        _lib = L
+    return _lib
+
+
+class EinsplineError(RuntimeError):
+    pass
+
+
+def check(ret=None):
+    """Raise EinsplineError if the last call left an error status."""
+    L = load()
+    code = L.einspline_gb300_last_error()
+    if code:
+        msg = L.einspline_gb300_last_error_message().decode()
+        L.einspline_gb300_clear_error()
+        raise EinsplineError(f"[{code}] {msg}")
+    return ret

@@ -1,0 +1,298 @@
+"""Python handles over the C-ABI (used by tests, the benchmark and smoke()).
+
+Mirrors the reference's uniform 3D multi-spline interface:
+``MultiUBspline3D`` wraps create/set/eval_multi_UBspline_3d_{s,d,c,z}
+(src/multi_bspline_create.c, src/multi_bspline_eval_std_*_impl.h) and
+``CudaSpline`` wraps create_multi_UBspline_3d_*_cuda plus
+eval_multi_multi_UBspline_3d_*[_vgh]_cuda (src/multi_bspline_create_cuda.cu,
+src/multi_bspline_cuda_*_impl.h).  Every call goes through
+libeinspline_gb300.so; torch is used only to hold device buffers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import (ANTIPERIODIC, DERIV1, DERIV2, FLAT, NATURAL, PERIODIC, STORE_BF16, STORE_F16,  # noqa: F401
+                   STORE_F32, STORE_F64, STORE_NATIVE, EinsplineError, check)
+
+_TYPE_CODE = {"s": L.SINGLE_REAL, "d": L.DOUBLE_REAL, "c": L.SINGLE_COMPLEX, "z": L.DOUBLE_COMPLEX}
+
+
+def _lib():
+    return L.load()
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def out_dtype(kind):
+    return np.float32 if kind in "sc" else np.float64
+
+
+def _bc(kind, b):
+    lc, rc, *v = b
+    v = list(v) + [0.0] * (4 - len(v))
+    BC = L.BC_TYPES[kind]
+    return BC(lc, rc, v[0], v[2]) if kind in "sd" else BC(lc, rc, v[0], v[1], v[2], v[3])
+
+
+class MultiUBspline3D:
+    """A uniform 3D multi-spline made by this library.
+
+    grids: three (start, end, num) tuples; bcs: three (lCode, rCode[, lVal_r,
+    lVal_i, rVal_r, rVal_i]) tuples; storage: one of STORE_* (s/c only)."""
+
+    def __init__(self, kind: str, grids, bcs, num_splines: int, storage: int = STORE_NATIVE):
+        lib = _lib()
+        self.kind = kind
+        self.N = num_splines
+        self.ncomp = 2 if kind in "cz" else 1
+        self.M = tuple(int(g[2]) for g in grids)
+        ug = [L.Ugrid(float(g[0]), float(g[1]), int(g[2]), 0.0, 0.0) for g in grids]
+        bc = [_bc(kind, b) for b in bcs]
+        if storage == STORE_NATIVE:
+            f = getattr(lib, f"create_multi_UBspline_3d_{kind}")
+            p = f(*ug, *bc, num_splines)
+        else:
+            if kind not in "sc":
+                raise ValueError("only s and c tables take a storage choice")
+            p = getattr(lib, f"einspline_gb300_create_3d_{kind}")(*ug, *bc, num_splines, storage)
+        check()
+        if not p:
+            raise EinsplineError("create failed")
+        self.ptr = p
+        self.table = C.c_void_p(p.contents.gb300)
+
+    # -- set ------------------------------------------------------------
+    def set(self, i: int, data) -> None:
+        """set_multi_UBspline_3d_*: data (Mx, My, Mz) real or complex/trailing-2 host array."""
+        dt = np.float32 if self.kind in "sc" else np.float64
+        d = np.asarray(data)
+        if self.ncomp == 2 and np.iscomplexobj(d):
+            d = np.stack([d.real, d.imag], axis=-1)
+        d = np.ascontiguousarray(d, dtype=dt)
+        getattr(_lib(), f"set_multi_UBspline_3d_{self.kind}")(self.ptr, i, d.ctypes.data)
+        check()
+
+    def set_device(self, first: int, data) -> None:
+        """Bulk set from a torch CUDA tensor [count, Mx, My, Mz(, 2)]."""
+        count = int(data.shape[0])
+        _lib().einspline_gb300_set_3d_device(self.table, first, count, C.c_void_p(data.data_ptr()))
+        check()
+
+    def flush(self) -> None:
+        _lib().einspline_gb300_flush(self.table)
+        check()
+
+    # -- info / table ----------------------------------------------------
+    def info(self) -> L.TableInfo:
+        ti = L.TableInfo()
+        _lib().einspline_gb300_get_table_info(self.table, C.byref(ti))
+        check()
+        return ti
+
+    def table_host(self):
+        """(table, scales): the stored table as numpy [Nx][Ny][Nz][ncol_pad]
+        of the storage type (float16 bit patterns for BF16 are uint16)."""
+        ti = self.info()
+        dt = {1: np.float32, 2: np.float16, 3: np.uint16, 4: np.float64}[ti.storage]
+        out = np.empty((ti.nx, ti.ny, ti.nz, ti.ncol_pad), dtype=dt)
+        sc = np.empty(ti.ncol, dtype=np.float32)
+        _lib().einspline_gb300_copy_table(self.table, out.ctypes.data, sc.ctypes.data)
+        check()
+        return out, sc
+
+    def table_values(self) -> np.ndarray:
+        """Dequantized table as float64 [Nx][Ny][Nz][N] (complex: [..., N, 2])."""
+        t, sc = self.table_host()
+        ti = self.info()
+        if ti.storage == STORE_BF16:
+            t = (t.astype(np.uint32) << 16).view(np.float32)
+        v = t[..., :ti.ncol].astype(np.float64) * sc.astype(np.float64)
+        if self.ncomp == 2:
+            v = v.reshape(v.shape[:3] + (self.N, 2))
+        return v
+
+    # -- tiles -----------------------------------------------------------
+    def set_tile(self, tx: int, ty: int, pb: int) -> None:
+        _lib().einspline_gb300_set_tile(self.table, tx, ty, pb)
+        check()
+
+    def get_tile(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _lib().einspline_gb300_get_tile(self.table, C.byref(a), C.byref(b), C.byref(c))
+        check()
+        return a.value, b.value, c.value
+
+    def autotune(self, npts: int, vgh: bool = True):
+        _lib().einspline_gb300_autotune(self.table, npts, int(vgh))
+        check()
+        return self.get_tile()
+
+    # -- evaluation --------------------------------------------------------
+    def eval_point(self, x: float, y: float, z: float, vgh: bool = True):
+        """eval_multi_UBspline_3d_*[_vgh] at one point, CPU layout."""
+        dt = out_dtype(self.kind)
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((self.N,) + ext, dt)
+        lib = _lib()
+        if vgh:
+            g = np.zeros((self.N, 3) + ext, dt)
+            h = np.zeros((self.N, 3, 3) + ext, dt)
+            getattr(lib, f"eval_multi_UBspline_3d_{self.kind}_vgh")(self.ptr, x, y, z, v.ctypes.data,
+                                                                    g.ctypes.data, h.ctypes.data)
+            check()
+            return v, g, h
+        getattr(lib, f"eval_multi_UBspline_3d_{self.kind}")(self.ptr, x, y, z, v.ctypes.data)
+        check()
+        return v, None, None
+
+    def out_shapes(self, P, layout):
+        ext = (2,) if self.ncomp == 2 else ()
+        if layout == 0:
+            if self.ncomp == 2:
+                return (P, self.N, 2), (P, self.N, 2, 3), (P, self.N, 2, 6)
+            return (P, self.N), (P, self.N, 3), (P, self.N, 6)
+        return (P, self.N) + ext, (P, self.N, 3) + ext, (P, self.N, 3, 3) + ext
+
+    def opts(self, vgh=True, pos_f64=True, rule=0, layout=0, sort=False, strides=(0, 0, 0)) -> L.EvalOpts:
+        return L.EvalOpts(int(vgh), int(pos_f64), rule, layout, int(sort), *strides)
+
+    def eval(self, pos, vgh=True, rule=0, layout=0, sort=False, out=None, stream=None):
+        """einspline_gb300_eval_3d on torch CUDA tensors.  pos: [P, 3]
+        float32/float64.  Returns (vals, grads, hess) torch tensors."""
+        torch = _torch()
+        P = int(pos.shape[0])
+        dt = torch.float32 if self.kind in "sc" else torch.float64
+        if out is None:
+            shp = self.out_shapes(P, layout)
+            out = (torch.empty(shp[0], dtype=dt, device=pos.device),
+                   torch.empty(shp[1], dtype=dt, device=pos.device) if vgh else None,
+                   torch.empty(shp[2], dtype=dt, device=pos.device) if vgh else None)
+        o = self.opts(vgh, pos.dtype == torch.float64, rule, layout, sort)
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)  # noqa: E731
+        s = C.c_void_p(stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream)
+        _lib().einspline_gb300_eval_3d(self.table, C.byref(o), P, ptr(pos), ptr(out[0]), ptr(out[1]),
+                                       ptr(out[2]), s)
+        check()
+        return out
+
+    def eval_host(self, pos: np.ndarray, vgh=True, rule=0, layout=0, out=None):
+        """einspline_gb300_eval_3d_host: host numpy buffers (pin them for speed)."""
+        P = pos.shape[0]
+        dt = out_dtype(self.kind)
+        if out is None:
+            shp = self.out_shapes(P, layout)
+            out = (np.empty(shp[0], dt), np.empty(shp[1], dt) if vgh else None,
+                   np.empty(shp[2], dt) if vgh else None)
+        o = self.opts(vgh, pos.dtype == np.float64, rule, layout)
+        ptr = lambda a: C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)  # noqa: E731
+        _lib().einspline_gb300_eval_3d_host(self.table, C.byref(o), P, ptr(pos), ptr(out[0]), ptr(out[1]),
+                                            ptr(out[2]))
+        check()
+        return out
+
+    # -- device handle -----------------------------------------------------
+    def to_cuda(self, storage=None) -> "CudaSpline":
+        lib = _lib()
+        if storage is None:
+            c = getattr(lib, f"create_multi_UBspline_3d_{self.kind}_cuda")(self.ptr)
+            kind = self.kind
+        elif storage == "conv":
+            assert self.kind in "dz"
+            kind = "s" if self.kind == "d" else "c"
+            c = getattr(lib, f"create_multi_UBspline_3d_{kind}_cuda_conv")(self.ptr)
+        else:
+            assert self.kind in "dz"
+            kind = "s" if self.kind == "d" else "c"
+            fn = "einspline_gb300_create_3d_s_cuda_from_d" if self.kind == "d" else \
+                "einspline_gb300_create_3d_c_cuda_from_z"
+            c = getattr(lib, fn)(self.ptr, storage)
+        check()
+        return CudaSpline(kind, c, self.N)
+
+    def destroy(self) -> None:
+        if getattr(self, "ptr", None):
+            _lib().destroy_Bspline(C.cast(self.ptr, C.c_void_p))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class CudaSpline:
+    """A device handle from create_multi_UBspline_3d_*_cuda[_conv]."""
+
+    def __init__(self, kind, ptr, N):
+        self.kind, self.ptr, self.N = kind, ptr, N
+        self.ncomp = 2 if kind in "cz" else 1
+        self.table = C.c_void_p(ptr.contents.gb300)
+
+    @property
+    def fields(self):
+        return self.ptr.contents
+
+    def eval_multi(self, pos, vgh=True, outs=None):
+        """eval_multi_multi_UBspline_3d_*[_vgh]_cuda with per-point output
+        pointer arrays built over contiguous torch buffers (GPU layout)."""
+        torch = _torch()
+        P = int(pos.shape[0])
+        dt = torch.float32 if self.kind in "sc" else torch.float64
+        nr = self.N * self.ncomp
+        if outs is None:
+            v = torch.zeros((P, nr), dtype=dt, device=pos.device)
+            g = torch.zeros((P, 3 * nr), dtype=dt, device=pos.device) if vgh else None
+            h = torch.zeros((P, 6 * nr), dtype=dt, device=pos.device) if vgh else None
+        else:
+            v, g, h = outs
+        es = v.element_size()
+
+        def ptrs(t, per):
+            base = t.data_ptr()
+            return torch.tensor([base + i * per * es for i in range(P)], dtype=torch.int64, device=pos.device)
+
+        vp = ptrs(v, v.shape[1])
+        lib = _lib()
+        if vgh:
+            gp, hp = ptrs(g, g.shape[1]), ptrs(h, h.shape[1])
+            getattr(lib, f"eval_multi_multi_UBspline_3d_{self.kind}_vgh_cuda")(
+                self.ptr, C.c_void_p(pos.data_ptr()), C.c_void_p(vp.data_ptr()), C.c_void_p(gp.data_ptr()),
+                C.c_void_p(hp.data_ptr()), P)
+        else:
+            getattr(lib, f"eval_multi_multi_UBspline_3d_{self.kind}_cuda")(
+                self.ptr, C.c_void_p(pos.data_ptr()), C.c_void_p(vp.data_ptr()), P)
+        check()
+        return v, g, h
+
+    def destroy(self):
+        if getattr(self, "ptr", None):
+            getattr(_lib(), f"destroy_multi_UBspline_3d_{self.kind}_cuda")(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def launch_count() -> int:
+    return int(_lib().einspline_gb300_launch_count())
+
+
+def fill_uniform(t, seed: int, lo: float = 0.0, hi: float = 1.0, offset: int = 0, stream=None):
+    """Fill a torch CUDA float32/float64 tensor with the splitmix64 uniform stream."""
+    torch = _torch()
+    s = C.c_void_p(stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream)
+    _lib().einspline_gb300_fill_uniform(C.c_void_p(t.data_ptr()), t.numel(), int(t.dtype == torch.float64),
+                                        seed & 0xFFFFFFFFFFFFFFFF, offset, lo, hi, s)
+    check()
+    return t

@@ -1,0 +1,330 @@
+// Library extensions: batched evaluation into flat device buffers on a
+// caller's stream, cell-sorted evaluation, a host-buffer entry with
+// copy/compute overlap, launch-shape control and autotuning, and the
+// device-side splitmix64 generator used for synthetic inputs.
+#include <cub/device/device_radix_sort.cuh>
+#include <limits.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+
+#include "eg_internal.h"
+
+namespace eg {
+
+// ------------------------------------------------------------------ sorting
+// Morton key of a point's cell (same cell rule as the evaluation) and its
+// index; sorting the pairs gives a visiting order in which consecutive
+// points share stencil rows.
+__device__ __forceinline__ uint64_t spread3(uint64_t v) {
+  v &= 0x1FFFFF;
+  v = (v | (v << 32)) & 0x1F00000000FFFFull;
+  v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+  v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+  v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+__global__ void k_cell_keys(const EvalArgs a, uint64_t *keys, int *idx) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npts) return;
+  int c[3];
+  for (int ax = 0; ax < 3; ax++) {
+    const double xd = a.pos_f64 ? reinterpret_cast<const double *>(a.pos)[3 * p + ax]
+                                : (double)reinterpret_cast<const float *>(a.pos)[3 * p + ax];
+    double u = (a.rule == 0) ? (xd - a.start[ax]) * a.dinv[ax] : xd * a.dinv[ax];
+    int i = (int)floor(u);
+    c[ax] = i < 0 ? 0 : (i > a.lim[ax] ? a.lim[ax] : i);
+  }
+  keys[p] = (spread3(c[0]) << 2) | (spread3(c[1]) << 1) | spread3(c[2]);
+  idx[p] = (int)p;
+}
+
+__global__ void k_iota(int *p, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = (int)i;
+}
+
+int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
+  const int64_t n = a.npts;
+  if (n > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "sorted evaluation takes at most %d points", INT_MAX);
+  int bits = 0;
+  for (int ax = 0; ax < 3; ax++) {
+    int b = 1;
+    while ((1 << b) <= a.lim[ax]) b++;
+    bits = std::max(bits, b);
+  }
+  const int end_bit = std::min(63, 3 * bits);
+  size_t temp = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, temp, (uint64_t *)nullptr, (uint64_t *)nullptr, (int *)nullptr,
+                                  (int *)nullptr, (int)n, 0, end_bit, s);
+  const size_t need = align_up_sz(n * 8, 256) * 2 + align_up_sz(n * 4, 256) * 2 + align_up_sz(temp, 256);
+  if (t->sort_bytes < need) {
+    cudaFree(t->sort_dev);
+    t->sort_dev = nullptr;
+    t->sort_bytes = 0;
+    if (cudaMalloc(&t->sort_dev, need) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(EINSPLINE_GB300_ENOMEM, "cannot allocate %zu bytes for point sorting", need);
+    }
+    t->sort_bytes = need;
+  }
+  char *p = (char *)t->sort_dev;
+  uint64_t *k_in = (uint64_t *)p; p += align_up_sz(n * 8, 256);
+  uint64_t *k_out = (uint64_t *)p; p += align_up_sz(n * 8, 256);
+  int *v_in = (int *)p; p += align_up_sz(n * 4, 256);
+  int *v_out = (int *)p; p += align_up_sz(n * 4, 256);
+  void *tmp = p;
+  k_cell_keys<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, k_in, v_in);
+  count_launch();
+  EG_CUDA(cudaGetLastError());
+  EG_CUDA(cub::DeviceRadixSort::SortPairs(tmp, temp, k_in, k_out, v_in, v_out, (int)n, 0, end_bit, s));
+  count_launch();
+  *perm_out = v_out;
+  return 0;
+}
+
+// ------------------------------------------------------------------ helpers
+__global__ void k_scale_box(double *pos, int64_t n, double lx, double ly, double lz) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  pos[3 * p] *= lx; pos[3 * p + 1] *= ly; pos[3 * p + 2] *= lz;
+}
+
+static int check_opts(Table *t, const einspline_gb300_eval_opts *o) {
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (!o) return fail(EINSPLINE_GB300_EINVAL, "opts is NULL");
+  if (o->rule < 0 || o->rule > 1 || o->layout < 0 || o->layout > 1)
+    return fail(EINSPLINE_GB300_EINVAL, "opts.rule and opts.layout must be 0 or 1");
+  return 0;
+}
+
+static void setup_args(Table *t, const einspline_gb300_eval_opts *o, EvalArgs &a) {
+  memset(&a, 0, sizeof(a));
+  fill_eval_geometry(t, a);
+  a.pos_f64 = o->pos_f64;
+  a.rule = o->rule;
+  a.layout = o->layout;
+  a.vstride = o->vstride ? o->vstride : t->ncol;
+  a.gstride = o->gstride ? o->gstride : 3 * (int64_t)t->ncol;
+  a.hstride = o->hstride ? o->hstride : (o->layout ? 9 : 6) * (int64_t)t->ncol;
+}
+
+static int eval_device(Table *t, const einspline_gb300_eval_opts *o, int64_t npts, const void *pos_d, void *v,
+                       void *g, void *h, cudaStream_t s) {
+  EvalArgs a;
+  setup_args(t, o, a);
+  a.npts = npts;
+  a.pos = pos_d;
+  a.vals = v; a.grads = g; a.hess = h;
+  if (o->sort && npts > 1) {
+    int *perm = nullptr;
+    if (int r = sort_points(t, a, &perm, s)) return r;
+    a.perm = perm;
+  }
+  int tx, ty, pb;
+  pick_tile(t, o->vgh != 0, npts, tx, ty, pb);
+  return launch_eval(t, a, o->vgh != 0, s, tx, ty, pb);
+}
+
+}  // namespace eg
+
+using namespace eg;
+
+extern "C" {
+
+int einspline_gb300_eval_3d(einspline_gb300_table *t, const einspline_gb300_eval_opts *o, int64_t npts,
+                            const void *pos_d, void *vals_d, void *grads_d, void *hess_d, void *stream) {
+  clear();
+  if (int r = check_opts(t, o)) return r;
+  if (npts < 0) return fail(EINSPLINE_GB300_EINVAL, "npts < 0");
+  if (npts == 0) return 0;
+  if (!pos_d || !vals_d || (o->vgh && (!grads_d || !hess_d)))
+    return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_eval_3d: NULL buffer");
+  if (int r = table_flush(t)) return r;
+  cudaStream_t s = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+  return eval_device(t, o, npts, pos_d, vals_d, grads_d, hess_d, s);
+}
+
+int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300_eval_opts *o, int64_t npts,
+                                 const void *pos_h, void *vals_h, void *grads_h, void *hess_h) {
+  clear();
+  if (int r = check_opts(t, o)) return r;
+  if (npts < 0) return fail(EINSPLINE_GB300_EINVAL, "npts < 0");
+  if (npts == 0) return 0;
+  if (!pos_h || !vals_h || (o->vgh && (!grads_h || !hess_h)))
+    return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_eval_3d_host: NULL buffer");
+  if (int r = table_flush(t)) return r;
+  std::lock_guard<std::mutex> lock(t->mu);
+  const size_t rb = t->storage == ST_F64 ? 8 : 4;
+  const int hq = o->layout ? 9 : 6;
+  const size_t per_pt_out = (size_t)t->ncol * rb * (o->vgh ? (4 + hq) : 1);
+  const size_t pos_b = o->pos_f64 ? 24 : 12;
+  // Chunks of about 64 MB of output, two in flight.
+  int64_t chunk = std::max<int64_t>(1, (int64_t)((64u << 20) / per_pt_out));
+  chunk = std::min(chunk, npts);
+  const size_t slot = align_up_sz(chunk * pos_b, 256) + align_up_sz(chunk * per_pt_out, 256);
+  if (t->pipe_bytes < 2 * slot) {
+    cudaFree(t->pipe_dev);
+    t->pipe_dev = nullptr;
+    t->pipe_bytes = 0;
+    if (cudaMalloc(&t->pipe_dev, 2 * slot) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(EINSPLINE_GB300_ENOMEM, "cannot allocate %zu bytes of pipeline buffers", 2 * slot);
+    }
+    t->pipe_bytes = 2 * slot;
+  }
+  for (int i = 0; i < 2; i++)
+    if (!t->pipe_stream[i]) EG_CUDA(cudaStreamCreateWithFlags(&t->pipe_stream[i], cudaStreamNonBlocking));
+  const int64_t vs = o->vstride ? o->vstride : t->ncol;
+  const int64_t gs = o->gstride ? o->gstride : 3 * (int64_t)t->ncol;
+  const int64_t hs = o->hstride ? o->hstride : hq * (int64_t)t->ncol;
+  einspline_gb300_eval_opts od = *o;
+  od.vstride = t->ncol; od.gstride = 3 * (int64_t)t->ncol; od.hstride = hq * (int64_t)t->ncol;
+  od.sort = 0;
+  int k = 0;
+  for (int64_t p0 = 0; p0 < npts; p0 += chunk, k++) {
+    const int64_t n = std::min(chunk, npts - p0);
+    cudaStream_t s = t->pipe_stream[k & 1];
+    char *base = (char *)t->pipe_dev + (size_t)(k & 1) * slot;
+    char *pos_d = base;
+    char *out_d = base + align_up_sz(chunk * pos_b, 256);
+    char *v_d = out_d;
+    char *g_d = v_d + (size_t)chunk * t->ncol * rb;
+    char *h_d = g_d + (size_t)chunk * 3 * t->ncol * rb;
+    EG_CUDA(cudaMemcpyAsync(pos_d, (const char *)pos_h + p0 * pos_b, n * pos_b, cudaMemcpyHostToDevice, s));
+    if (int r = eval_device(t, &od, n, pos_d, v_d, g_d, h_d, s)) return r;
+    EG_CUDA(cudaMemcpy2DAsync((char *)vals_h + p0 * vs * rb, vs * rb, v_d, t->ncol * rb, t->ncol * rb, n,
+                              cudaMemcpyDeviceToHost, s));
+    if (o->vgh) {
+      EG_CUDA(cudaMemcpy2DAsync((char *)grads_h + p0 * gs * rb, gs * rb, g_d, 3 * t->ncol * rb, 3 * t->ncol * rb, n,
+                                cudaMemcpyDeviceToHost, s));
+      EG_CUDA(cudaMemcpy2DAsync((char *)hess_h + p0 * hs * rb, hs * rb, h_d, hq * t->ncol * rb, hq * t->ncol * rb, n,
+                                cudaMemcpyDeviceToHost, s));
+    }
+  }
+  EG_CUDA(cudaStreamSynchronize(t->pipe_stream[0]));
+  EG_CUDA(cudaStreamSynchronize(t->pipe_stream[1]));
+  return 0;
+}
+
+int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb) {
+  clear();
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (tx == 0 && ty == 0 && pb == 0) { t->tile_tx = t->tile_ty = t->tile_pb = 0; return 0; }
+  if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
+    return fail(EINSPLINE_GB300_EINVAL, "tile must have tx a multiple of 32, tx*ty <= 256, 1 <= pb <= 64");
+  t->tile_tx = tx; t->tile_ty = ty; t->tile_pb = pb;
+  return 0;
+}
+
+int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb) {
+  clear();
+  if (!table_ok(t) || !tx || !ty || !pb) return fail(EINSPLINE_GB300_EINVAL, "bad argument");
+  pick_tile(t, true, 0, *tx, *ty, *pb);
+  return 0;
+}
+
+int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
+  clear();
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (npts < 1) return fail(EINSPLINE_GB300_EINVAL, "npts must be >= 1");
+  if (int r = table_flush(t)) return r;
+  const size_t rb = t->storage == ST_F64 ? 8 : 4;
+  const size_t out_b = (size_t)npts * t->ncol * rb * (vgh ? 10 : 1);
+  void *buf = nullptr;
+  if (cudaMalloc(&buf, out_b + (size_t)npts * 24) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(EINSPLINE_GB300_ENOMEM, "autotune scratch");
+  }
+  double *pos = (double *)((char *)buf + out_b);
+  // Points uniform in the box: unit draws, scaled per axis by the cell rule
+  // below (rule 1 measures positions from the grid origin).
+  einspline_gb300_fill_uniform(pos, 3 * npts, 1, 0x5eed5eedull, 0, 0.0, 1.0, t->stream);
+  k_scale_box<<<(unsigned)((npts + 255) / 256), 256, 0, t->stream>>>(pos, npts, t->end[0] - t->start[0],
+                                                                     t->end[1] - t->start[1], t->end[2] - t->start[2]);
+  count_launch();
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  fill_eval_geometry(t, a);
+  a.pos = pos;
+  a.pos_f64 = 1;
+  a.rule = 1;
+  a.layout = 0;
+  a.npts = npts;
+  a.vals = buf;
+  a.grads = (char *)buf + (size_t)npts * t->ncol * rb;
+  a.hess = (char *)buf + (size_t)npts * 4 * t->ncol * rb;
+  a.vstride = t->ncol; a.gstride = 3 * (int64_t)t->ncol; a.hstride = 6 * (int64_t)t->ncol;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int btx = 0, bty = 0, bpb = 0;
+  const int VW = elems_per_thread(t);
+  const int need = (t->ncol + VW - 1) / VW;
+  for (int tx = 32; tx <= 256; tx *= 2) {
+    if (tx > 32 && (tx / 2) * VW >= t->ncol) break;  // wider tiles only idle threads
+    for (int ty = 1; tx * ty <= 256; ty *= 2)
+      for (int m = 1; m <= 8; m *= 2) {
+        const int pb = ty * m;
+        if (pb > 64) continue;
+        EvalArgs b = a;
+        if (launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb)) { cudaFree(buf); return einspline_gb300_last_error(); }
+        cudaEventRecord(e0, t->stream);
+        for (int r = 0; r < 3; r++) {
+          b = a;
+          launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb);
+        }
+        cudaEventRecord(e1, t->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) { best = ms; btx = tx; bty = ty; bpb = pb; }
+      }
+  }
+  (void)need;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaError_t e = cudaStreamSynchronize(t->stream);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_check(e, "autotune");
+  const int v = vgh ? 1 : 0;
+  t->tuned_tx[v] = btx; t->tuned_ty[v] = bty; t->tuned_pb[v] = bpb;
+  return 0;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ synth
+namespace {
+__global__ void k_fill_uniform(void *dst, int64_t n, int f64, uint64_t seed, int64_t offset, double lo, double hi) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t z = seed + (uint64_t)(offset + i + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  const double u = __dmul_rn((double)(z >> 11), 1.0 / 9007199254740992.0);
+  const double v = __dadd_rn(lo, __dmul_rn(__dsub_rn(hi, lo), u));
+  if (f64) ((double *)dst)[i] = v;
+  else ((float *)dst)[i] = __double2float_rn(v);
+}
+}  // namespace
+
+extern "C" int einspline_gb300_fill_uniform(void *dst_d, int64_t n, int f64, uint64_t seed, int64_t offset, double lo,
+                                            double hi, void *stream) {
+  clear();
+  if (!dst_d || n < 0) return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_fill_uniform: bad argument");
+  if (n == 0) return 0;
+  const int64_t blocks = (n + 255) / 256;
+  if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "fill too large");
+  k_fill_uniform<<<(unsigned)blocks, 256, 0, stream ? (cudaStream_t)stream : cudaStreamLegacy>>>(dst_d, n, f64, seed,
+                                                                                                 offset, lo, hi);
+  count_launch();
+  EG_CUDA(cudaGetLastError());
+  return 0;
+}

@@ -1,0 +1,175 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "einspline_gb300.h"
+
+namespace eg {
+
+constexpr uint32_t kMagic = 0x45473330u;  // "EG30"
+
+enum Storage { ST_NATIVE = 0, ST_F32 = 1, ST_F16 = 2, ST_BF16 = 3, ST_F64 = 4 };
+
+// ---------------------------------------------------------------- errors
+// Records a status for the calling thread; aborts when abort mode is on.
+int fail(int code, const char *fmt, ...);
+void clear();
+// Checks a CUDA status; records and returns ECUDA on failure.
+int cuda_check(cudaError_t e, const char *what);
+#define EG_CUDA(call)                                                  \
+  do {                                                                 \
+    cudaError_t eg_e_ = (call);                                        \
+    if (eg_e_ != cudaSuccess) return ::eg::cuda_check(eg_e_, #call);   \
+  } while (0)
+void count_launch(int n = 1);
+inline size_t align_up_sz(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// --------------------------------------------------------- line factors
+// Data-independent part of the 1D interpolation solve for one axis, found
+// once on the host by running the reference elimination on the band
+// coefficients alone.  The device kernels then only push right-hand sides
+// through the recorded multipliers and divisors, in the reference's order.
+struct LineFactors {
+  int M = 0;
+  int cyclic = 1;   // periodic/antiperiodic (1) or boundary-row system (0)
+  int anti = 0;     // antiperiodic wrap sign
+  int lcode = 0, rcode = 0;
+  // Packed arrays, each of length M+2:
+  //  cyclic: P (divisors), L (sub-diagonal multipliers), E (last-row
+  //          multipliers), U (super-diagonal), LC (wrap column); scalars F, Q
+  //  bc:     P, L, U; scalars R0, R1, Q (last row), U0a, U0b (first row),
+  //          and the boundary rows' own divisor P[0]
+  std::vector<double> P, L, E, U, LC;
+  double F = 0, Q = 0, R0 = 0, R1 = 0, U0a = 0, U0b = 0;
+};
+void build_line_factors(int M, int lcode, int rcode, double delta_inv, LineFactors &f);
+// Offsets of the arrays inside the packed device copy.
+struct PackedFactors {
+  int M, cyclic, anti, pad_;
+  double F, Q, R0, R1, U0a, U0b;
+};
+size_t packed_factor_doubles(int M);
+void pack_line_factors(const LineFactors &f, std::vector<double> &out);
+
+// ----------------------------------------------------------------- table
+}  // namespace eg
+
+struct einspline_gb300_table {
+  uint32_t magic = eg::kMagic;
+  char kind = 's';        // 's','d','c','z'
+  int storage = eg::ST_F32;
+  int ncomp = 1;          // 1 real, 2 complex
+  int num_splines = 0;
+  int ncol = 0;           // ncomp * num_splines real columns
+  int ncol_pad = 0;       // real columns per stored row (128-byte rows)
+  int elem_bytes = 4;
+  int M[3] = {0, 0, 0};   // data points per axis
+  int Nc[3] = {0, 0, 0};  // coefficients per axis
+  double start[3], end[3], delta[3], dinv[3];
+  int lcode[3], rcode[3];
+  double lval[3][2], rval[3][2];
+  int64_t xs = 0, ys = 0, zs = 0;  // strides in stored reals
+  size_t table_bytes = 0;
+  void *coefs = nullptr;            // device
+  float *scale = nullptr;           // device, ncol_pad floats (F16/BF16)
+  bool owns = true;
+
+  // queued set calls
+  std::mutex mu;
+  int cap = 0;                      // splines per batched solve
+  std::vector<int> pend_spline;     // slot -> spline index
+  std::unordered_map<int, int> slot_of;
+  void *staging = nullptr;          // device, cap * points * ncomp values of the input type
+  int in_bytes = 4;                 // bytes per input real (4 for s/c, 8 for d/z)
+  double *work_a = nullptr;         // device FP64 [Mx][My][Mz][cap*ncomp]
+  double *work_w = nullptr;         // device FP64 [Nx][Ny][Nz][cap*ncomp]
+  float *colmax = nullptr;          // device, cap*ncomp
+  int *slot_spline_d = nullptr;     // device, cap
+  double *factors_d = nullptr;      // device, 3 packed factor sets
+  size_t factor_off[3] = {0, 0, 0};
+  cudaStream_t stream = nullptr;
+
+  // single-point entry scratch
+  void *pt_dev = nullptr;           // device, 13 * ncol output reals
+  void *pt_host = nullptr;          // pinned host copy
+
+  // host-buffer pipeline scratch (einspline_gb300_eval_3d_host)
+  void *pipe_dev = nullptr;
+  size_t pipe_bytes = 0;
+  cudaStream_t pipe_stream[2] = {nullptr, nullptr};
+  cudaEvent_t pipe_event[2] = {nullptr, nullptr};
+
+  // cell-sorted evaluation scratch
+  void *sort_dev = nullptr;
+  size_t sort_bytes = 0;
+
+  // launch shape
+  int tile_tx = 0, tile_ty = 0, tile_pb = 0;
+  int tuned_tx[2] = {0, 0}, tuned_ty[2] = {0, 0}, tuned_pb[2] = {0, 0};
+};
+
+namespace eg {
+
+using Table = einspline_gb300_table;
+
+struct GridDesc {
+  double start, end;
+  int num;
+  int lcode, rcode;
+  double lval[2], rval[2];
+};
+
+// Creates a table object with its device storage (zero-filled).
+Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage);
+void table_destroy(Table *t);
+// Copy of src converted to another storage (device to device), with new
+// private storage; used by the *_cuda creators.
+Table *table_clone(Table *src, int storage);
+// Queue set calls; data on host (from_device=0) or device.
+int table_set(Table *t, int first, int count, const void *data, bool from_device);
+int table_flush(Table *t);
+inline bool table_ok(const Table *t) { return t && t->magic == kMagic; }
+
+// ---------------------------------------------------------------- eval
+struct EvalArgs {
+  const void *coefs;
+  const float *scale;
+  int64_t xs, ys, zs;         // stored reals
+  int ncol;                   // real columns to evaluate
+  int ncol_pad;
+  int lim[3];                 // largest first-cell index per axis (N-4)
+  double start[3], dinv[3];
+  float dinvf[3];
+  const void *pos;            // device positions (or null: inline)
+  double inl[3];              // inline position for the single-point entry
+  int pos_f64;
+  int rule;                   // 0 CPU-entry rule, 1 reference GPU rule
+  const int *perm;            // optional visiting order
+  int64_t npts;
+  // outputs: pointer arrays (per point) or flat bases with strides
+  void *const *vals_pp;
+  void *const *grads_pp;
+  void *const *hess_pp;
+  void *vals, *grads, *hess;
+  int64_t vstride, gstride, hstride;
+  int layout;                 // 0 GPU layout, 1 CPU layout
+  int is_complex;
+  int ntiles;                 // column tiles per point group
+  int pb;                     // points per block
+};
+
+int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb);
+void fill_eval_geometry(const Table *t, EvalArgs &a);
+void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb);
+int elems_per_thread(const Table *t);
+
+// sorting
+int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s);
+
+}  // namespace eg

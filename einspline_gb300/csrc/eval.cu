@@ -1,0 +1,591 @@
+// Evaluation kernels: value and value+gradient+Hessian of every spline of a
+// uniform 3D multi-spline at many points (src/multi_bspline_cuda_s_impl.h:179
+// and :343 for the batched GPU entries, src/multi_bspline_eval_std_s_impl.h:480
+// and :740 for the CPU entries; d, c, z alike).
+//
+// Work split: a block owns pb points and a tile of tx*VW consecutive real
+// columns (splines, or re/im halves of complex splines).  Each thread owns VW
+// consecutive columns and reads every stencil row with one 16-byte (FP32,
+// FP64) or 8-byte (FP16/BF16) load, so a warp reads 512/256 contiguous bytes
+// per row.  Cell and basis weights of the block's points are computed once
+// in a prologue and kept in shared memory.  The 64-row stencil is reduced
+// separably -- z first (3 sums per row pair), then y (6), then x (10) -- 328
+// multiply-adds per column and point instead of 640; the order does not
+// depend on the tile shape, so a point's results are bit-identical whichever
+// block or batch evaluates it.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <limits.h>
+#include <string.h>
+
+#include "eg_internal.h"
+
+namespace eg {
+
+// ------------------------------------------------------------ coefficient types
+template <int ST> struct CT;
+template <> struct CT<ST_F32> {
+  using A = float;
+  static constexpr int VW = 4, BYTES = 4;
+  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
+    const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+  }
+};
+template <> struct CT<ST_F16> {
+  using A = float;
+  static constexpr int VW = 4, BYTES = 2;
+  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
+    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(p));
+    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&x.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&x.y));
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+};
+template <> struct CT<ST_BF16> {
+  using A = float;
+  static constexpr int VW = 4, BYTES = 2;
+  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
+    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(p));
+    v[0] = __uint_as_float(x.x << 16); v[1] = __uint_as_float(x.x & 0xFFFF0000u);
+    v[2] = __uint_as_float(x.y << 16); v[3] = __uint_as_float(x.y & 0xFFFF0000u);
+  }
+};
+template <> struct CT<ST_F64> {
+  using A = double;
+  static constexpr int VW = 2, BYTES = 8;
+  __device__ static __forceinline__ void load(const char *p, double (&v)[2]) {
+    const double2 x = __ldg(reinterpret_cast<const double2 *>(p));
+    v[0] = x.x; v[1] = x.y;
+  }
+};
+
+int elems_per_thread(const Table *t) { return t->storage == ST_F64 ? 2 : 4; }
+static int acc_bytes(const Table *t) { return t->storage == ST_F64 ? 8 : 4; }
+
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+
+// Cubic B-spline basis at offset t: w[0..3] values, w[4..7] first and
+// w[8..11] second derivatives (the 4x4 power-basis matrices of
+// src/bspline_data.c:143-162 in Horner form).
+template <typename A>
+__device__ __forceinline__ void bspline_weights(A t, A *w) {
+  const A s6 = A(1) / A(6), t2 = t * t;
+  w[0] = fmaT(fmaT(fmaT(-s6, t, A(0.5)), t, A(-0.5)), t, s6);
+  w[1] = fmaT(fmaT(A(0.5), t, A(-1)), t2, A(2) / A(3));
+  w[2] = fmaT(fmaT(fmaT(A(-0.5), t, A(0.5)), t, A(0.5)), t, s6);
+  w[3] = s6 * t2 * t;
+  w[4] = fmaT(fmaT(A(-0.5), t, A(1)), t, A(-0.5));
+  w[5] = fmaT(A(1.5), t, A(-2)) * t;
+  w[6] = fmaT(fmaT(A(-1.5), t, A(1)), t, A(0.5));
+  w[7] = A(0.5) * t2;
+  w[8] = A(1) - t;
+  w[9] = fmaT(A(3), t, A(-2));
+  w[10] = fmaT(A(-3), t, A(1));
+  w[11] = t;
+}
+
+// Cell index and offset along one axis.
+//  rule 0 (CPU entries, src/multi_bspline_eval_std_s_impl.h:746-755):
+//    u = (x - start) * delta_inv, rounded to float for FP32 tables;
+//    i = trunc(u), t = u - i (modf).  Outside the table the edge cell is
+//    extrapolated (the reference reads out of bounds there).
+//  rule 1 (GPU entries, src/multi_bspline_cuda_s_impl.h:370-384):
+//    u = r * delta_inv (no start offset), i = clamp(floor(u), 0, dim-1),
+//    t = u - floor(u).
+__device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &idx, float &t) {
+  const int lim = a.lim[ax];
+  if (a.rule == 0) {
+    const float u = __double2float_rn(__dmul_rn(__dsub_rn(xd, a.start[ax]), a.dinv[ax]));
+    const float ip = truncf(u);
+    float tt = __fsub_rn(u, ip);
+    int i = (int)ip;
+    if (i < 0) { tt = __fadd_rn(tt, (float)i); i = 0; }
+    if (i > lim) { tt = __fadd_rn(tt, (float)(i - lim)); i = lim; }
+    idx = i; t = tt;
+  } else {
+    const float s = __fmul_rn((float)xd, a.dinvf[ax]);
+    const float sf = floorf(s);
+    int i = (int)sf;
+    i = i < 0 ? 0 : (i > lim ? lim : i);
+    idx = i; t = __fsub_rn(s, sf);
+  }
+}
+__device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &idx, double &t) {
+  const int lim = a.lim[ax];
+  if (a.rule == 0) {
+    const double u = __dmul_rn(__dsub_rn(xd, a.start[ax]), a.dinv[ax]);
+    const double ip = trunc(u);
+    double tt = __dsub_rn(u, ip);
+    int i = (int)ip;
+    if (i < 0) { tt = __dadd_rn(tt, (double)i); i = 0; }
+    if (i > lim) { tt = __dadd_rn(tt, (double)(i - lim)); i = lim; }
+    idx = i; t = tt;
+  } else {
+    const double s = __dmul_rn(xd, a.dinv[ax]);
+    const double sf = floor(s);
+    int i = (int)sf;
+    i = i < 0 ? 0 : (i > lim ? lim : i);
+    idx = i; t = __dsub_rn(s, sf);
+  }
+}
+
+// Separable reduction of the 4x4x4 stencil for VW columns.
+// w: [0..11] x weights, [12..23] y weights, [24..35] z weights.
+// o: v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz.
+template <int ST, bool VGH>
+__device__ __forceinline__ void contract(const char *base, int64_t xsb, int64_t ysb, int64_t zsb,
+                                         const typename CT<ST>::A *w, typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
+  using A = typename CT<ST>::A;
+  constexpr int VW = CT<ST>::VW;
+#pragma unroll
+  for (int q = 0; q < 10; q++)
+#pragma unroll
+    for (int e = 0; e < VW; e++) o[q][e] = A(0);
+  A wz[3][4];
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) wz[d][k] = w[24 + 4 * d + k];
+#pragma unroll 1
+  for (int i = 0; i < 4; i++) {
+    A y[6][VW];
+#pragma unroll
+    for (int q = 0; q < 6; q++)
+#pragma unroll
+      for (int e = 0; e < VW; e++) y[q][e] = A(0);
+    const char *plane = base + i * xsb;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      A c[4][VW];
+#pragma unroll
+      for (int k = 0; k < 4; k++) CT<ST>::load(plane + j * ysb + k * zsb, c[k]);
+      const A by = w[12 + j], dby = w[16 + j], d2by = w[20 + j];
+#pragma unroll
+      for (int e = 0; e < VW; e++) {
+        A z0 = c[0][e] * wz[0][0];
+        z0 = fmaT(c[1][e], wz[0][1], z0);
+        z0 = fmaT(c[2][e], wz[0][2], z0);
+        z0 = fmaT(c[3][e], wz[0][3], z0);
+        y[0][e] = fmaT(by, z0, y[0][e]);
+        if (VGH) {
+          A z1 = c[0][e] * wz[1][0];
+          z1 = fmaT(c[1][e], wz[1][1], z1);
+          z1 = fmaT(c[2][e], wz[1][2], z1);
+          z1 = fmaT(c[3][e], wz[1][3], z1);
+          A z2 = c[0][e] * wz[2][0];
+          z2 = fmaT(c[1][e], wz[2][1], z2);
+          z2 = fmaT(c[2][e], wz[2][2], z2);
+          z2 = fmaT(c[3][e], wz[2][3], z2);
+          y[1][e] = fmaT(dby, z0, y[1][e]);
+          y[2][e] = fmaT(d2by, z0, y[2][e]);
+          y[3][e] = fmaT(by, z1, y[3][e]);
+          y[4][e] = fmaT(dby, z1, y[4][e]);
+          y[5][e] = fmaT(by, z2, y[5][e]);
+        }
+      }
+    }
+    const A ax = w[i], dax = w[4 + i], d2ax = w[8 + i];
+#pragma unroll
+    for (int e = 0; e < VW; e++) {
+      o[0][e] = fmaT(ax, y[0][e], o[0][e]);
+      if (VGH) {
+        o[1][e] = fmaT(dax, y[0][e], o[1][e]);
+        o[2][e] = fmaT(ax, y[1][e], o[2][e]);
+        o[3][e] = fmaT(ax, y[3][e], o[3][e]);
+        o[4][e] = fmaT(d2ax, y[0][e], o[4][e]);
+        o[5][e] = fmaT(dax, y[1][e], o[5][e]);
+        o[6][e] = fmaT(dax, y[3][e], o[6][e]);
+        o[7][e] = fmaT(ax, y[2][e], o[7][e]);
+        o[8][e] = fmaT(ax, y[4][e], o[8][e]);
+        o[9][e] = fmaT(ax, y[5][e], o[9][e]);
+      }
+    }
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void st_vec(float *p, const float (&v)[N]) {
+#pragma unroll
+  for (int c = 0; c < N / 4; c++)
+    __stcs(reinterpret_cast<float4 *>(p) + c, make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]));
+}
+template <int N>
+__device__ __forceinline__ void st_vec(double *p, const double (&v)[N]) {
+#pragma unroll
+  for (int c = 0; c < N / 2; c++) __stcs(reinterpret_cast<double2 *>(p) + c, make_double2(v[2 * c], v[2 * c + 1]));
+}
+__device__ __forceinline__ bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// Index of Hessian entry m (row-major 3x3) among (xx, xy, xz, yy, yz, zz).
+__device__ __forceinline__ int h9to6(int m) {
+  return (m == 0) ? 0 : (m == 1 || m == 3) ? 1 : (m == 2 || m == 6) ? 2 : (m == 4) ? 3 : (m == 5 || m == 7) ? 4 : 5;
+}
+
+template <int ST, bool VGH>
+__device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col0,
+                                         typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
+  using A = typename CT<ST>::A;
+  constexpr int VW = CT<ST>::VW;
+  if (a.scale) {
+    const float4 s4 = *reinterpret_cast<const float4 *>(a.scale + col0);
+    const float sc[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+    for (int q = 0; q < (VGH ? 10 : 1); q++)
+#pragma unroll
+      for (int e = 0; e < VW; e++) o[q][e] *= (A)sc[e];
+  }
+  if (VGH) {
+    A dx, dy, dz;
+    if (sizeof(A) == 4) { dx = (A)a.dinvf[0]; dy = (A)a.dinvf[1]; dz = (A)a.dinvf[2]; }
+    else { dx = (A)a.dinv[0]; dy = (A)a.dinv[1]; dz = (A)a.dinv[2]; }
+    const A f[10] = {A(1), dx, dy, dz, dx * dx, dx * dy, dx * dz, dy * dy, dy * dz, dz * dz};
+#pragma unroll
+    for (int q = 1; q < 10; q++)
+#pragma unroll
+      for (int e = 0; e < VW; e++) o[q][e] *= f[q];
+  }
+  A *vp = a.vals_pp ? (A *)a.vals_pp[src] : (A *)a.vals + src * a.vstride;
+  const bool full = col0 + VW <= a.ncol;
+  {
+    A v[VW];
+#pragma unroll
+    for (int e = 0; e < VW; e++) v[e] = o[0][e];
+    if (full && al16(vp + col0)) st_vec<VW>(vp + col0, v);
+    else
+#pragma unroll
+      for (int e = 0; e < VW; e++)
+        if (col0 + e < a.ncol) vp[col0 + e] = v[e];
+  }
+  if (!VGH) return;
+  A *gp = a.grads_pp ? (A *)a.grads_pp[src] : (A *)a.grads + src * a.gstride;
+  A *hp = a.hess_pp ? (A *)a.hess_pp[src] : (A *)a.hess + src * a.hstride;
+  const bool cpx_cpu = a.is_complex && a.layout == 1;
+  {
+    A g[3 * VW];
+#pragma unroll
+    for (int e = 0; e < VW; e++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const int idx = cpx_cpu ? 6 * (e >> 1) + 2 * c + (e & 1) : 3 * e + c;
+        g[idx] = o[1 + c][e];
+      }
+    A *gb = gp + 3 * (int64_t)col0;
+    if (full && al16(gb)) st_vec<3 * VW>(gb, g);
+    else
+#pragma unroll
+      for (int e = 0; e < VW; e++)
+        if (col0 + e < a.ncol)
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const int idx = cpx_cpu ? 6 * (e >> 1) + 2 * c + (e & 1) : 3 * e + c;
+            gb[idx] = g[idx];
+          }
+  }
+  if (a.layout == 0) {
+    A h[6 * VW];
+#pragma unroll
+    for (int e = 0; e < VW; e++)
+#pragma unroll
+      for (int q = 0; q < 6; q++) h[6 * e + q] = o[4 + q][e];
+    A *hb = hp + 6 * (int64_t)col0;
+    if (full && al16(hb)) st_vec<6 * VW>(hb, h);
+    else
+#pragma unroll
+      for (int e = 0; e < VW; e++)
+        if (col0 + e < a.ncol)
+#pragma unroll
+          for (int q = 0; q < 6; q++) hb[6 * e + q] = h[6 * e + q];
+  } else {
+    A h[9 * VW];
+#pragma unroll
+    for (int e = 0; e < VW; e++)
+#pragma unroll
+      for (int m = 0; m < 9; m++) {
+        const int idx = a.is_complex ? 18 * (e >> 1) + 2 * m + (e & 1) : 9 * e + m;
+        h[idx] = o[4 + h9to6(m)][e];
+      }
+    A *hb = hp + 9 * (int64_t)col0;
+    if (full && al16(hb)) st_vec<9 * VW>(hb, h);
+    else
+#pragma unroll
+      for (int e = 0; e < VW; e++)
+        if (col0 + e < a.ncol)
+#pragma unroll
+          for (int m = 0; m < 9; m++) {
+            const int idx = a.is_complex ? 18 * (e >> 1) + 2 * m + (e & 1) : 9 * e + m;
+            hb[idx] = h[idx];
+          }
+  }
+}
+
+__host__ __device__ __forceinline__ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Shared memory: pb * 36 weights, pb * 3 cell indices, pb source indices.
+__host__ __device__ __forceinline__ size_t smem_w_bytes(int pb, int accb) { return align_up((size_t)pb * 36 * accb, 16); }
+__host__ __device__ __forceinline__ size_t smem_total(int pb, int accb) {
+  return smem_w_bytes(pb, accb) + align_up((size_t)pb * 3 * 4, 8) + (size_t)pb * 8;
+}
+
+template <int ST, bool VGH>
+__global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
+  using A = typename CT<ST>::A;
+  constexpr int VW = CT<ST>::VW;
+  extern __shared__ __align__(16) unsigned char smem[];
+  A *sw = reinterpret_cast<A *>(smem);
+  int *sidx = reinterpret_cast<int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
+  int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
+
+  const int tile = blockIdx.x % a.ntiles;
+  const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
+  const int pn = (int)min((int64_t)a.pb, a.npts - p0);
+  const int nthr = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  for (int q = tid; q < pn * 3; q += nthr) {
+    const int pp = q / 3, ax = q - 3 * pp;
+    const int64_t src = a.perm ? (int64_t)a.perm[p0 + pp] : p0 + pp;
+    double xd;
+    if (!a.pos) xd = a.inl[ax];
+    else if (a.pos_f64) xd = reinterpret_cast<const double *>(a.pos)[3 * src + ax];
+    else xd = (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
+    int idx;
+    A t;
+    cell(a, ax, xd, idx, t);
+    bspline_weights<A>(t, sw + pp * 36 + ax * 12);
+    sidx[pp * 3 + ax] = idx;
+    if (ax == 0) ssrc[pp] = src;
+  }
+  __syncthreads();
+
+  const int col0 = (tile * blockDim.x + threadIdx.x) * VW;
+  if (col0 >= a.ncol) return;
+  const char *cbase = reinterpret_cast<const char *>(a.coefs) + (int64_t)col0 * CT<ST>::BYTES;
+  const int64_t xsb = a.xs * CT<ST>::BYTES, ysb = a.ys * CT<ST>::BYTES, zsb = a.zs * CT<ST>::BYTES;
+  for (int pp = threadIdx.y; pp < pn; pp += blockDim.y) {
+    const char *base = cbase + sidx[3 * pp] * xsb + sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
+    A o[10][VW];
+    contract<ST, VGH>(base, xsb, ysb, zsb, sw + pp * 36, o);
+    epilogue<ST, VGH>(a, ssrc[pp], col0, o);
+  }
+}
+
+void fill_eval_geometry(const Table *t, EvalArgs &a) {
+  a.coefs = t->coefs;
+  a.scale = t->scale;
+  a.xs = t->xs; a.ys = t->ys; a.zs = t->zs;
+  a.ncol = t->ncol;
+  a.ncol_pad = t->ncol_pad;
+  for (int i = 0; i < 3; i++) {
+    a.lim[i] = t->Nc[i] - 4;
+    a.start[i] = t->start[i];
+    a.dinv[i] = t->dinv[i];
+    a.dinvf[i] = (float)t->dinv[i];
+  }
+  a.is_complex = t->ncomp == 2;
+}
+
+template <int ST, bool VGH>
+static cudaError_t launch_k(const EvalArgs &a, unsigned grid, dim3 block, size_t smem, cudaStream_t s) {
+  k_eval<ST, VGH><<<grid, block, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb) {
+  if (a.npts <= 0) return 0;
+  if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
+    return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
+  const int VW = elems_per_thread(t);
+  a.pb = pb;
+  a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
+  const int64_t npg = (a.npts + pb - 1) / pb;
+  const int64_t blocks = npg * a.ntiles;
+  if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
+  const size_t smem = smem_total(pb, acc_bytes(t));
+  dim3 block(tx, ty);
+  cudaError_t e;
+  switch (t->storage) {
+    case ST_F32: e = vgh ? launch_k<ST_F32, true>(a, (unsigned)blocks, block, smem, s)
+                         : launch_k<ST_F32, false>(a, (unsigned)blocks, block, smem, s); break;
+    case ST_F16: e = vgh ? launch_k<ST_F16, true>(a, (unsigned)blocks, block, smem, s)
+                         : launch_k<ST_F16, false>(a, (unsigned)blocks, block, smem, s); break;
+    case ST_BF16: e = vgh ? launch_k<ST_BF16, true>(a, (unsigned)blocks, block, smem, s)
+                          : launch_k<ST_BF16, false>(a, (unsigned)blocks, block, smem, s); break;
+    default: e = vgh ? launch_k<ST_F64, true>(a, (unsigned)blocks, block, smem, s)
+                     : launch_k<ST_F64, false>(a, (unsigned)blocks, block, smem, s); break;
+  }
+  count_launch();
+  if (e != cudaSuccess) return cuda_check(e, "evaluation kernel launch");
+  return 0;
+}
+
+void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb) {
+  if (t->tile_tx) { tx = t->tile_tx; ty = t->tile_ty; pb = t->tile_pb; return; }
+  const int v = vgh ? 1 : 0;
+  if (t->tuned_tx[v]) { tx = t->tuned_tx[v]; ty = t->tuned_ty[v]; pb = t->tuned_pb[v]; return; }
+  const int VW = elems_per_thread(t);
+  const int need = (t->ncol + VW - 1) / VW;
+  tx = (need + 31) / 32 * 32;
+  if (tx > 256) tx = 256;
+  ty = 256 / tx;
+  if (ty > 8) ty = 8;
+  pb = 2 * ty;
+  (void)npts;
+}
+
+}  // namespace eg
+
+using namespace eg;
+
+namespace {
+
+template <typename S>
+Table *host_table(S *s, const char *fn) {
+  if (!s || !table_ok(s->gb300)) {
+    fail(EINSPLINE_GB300_EINVAL, "%s: not a spline made by this library", fn);
+    return nullptr;
+  }
+  return s->gb300;
+}
+
+// Single point, host outputs in the CPU layout.
+template <typename S, typename V>
+void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, bool vgh, const char *fn) {
+  clear();
+  Table *t = host_table(s, fn);
+  if (!t) return;
+  if (table_flush(t)) return;
+  std::lock_guard<std::mutex> g(t->mu);
+  const size_t rb = acc_bytes(t);
+  const size_t n = (size_t)t->ncol;
+  const size_t bytes = (vgh ? 13 : 1) * n * rb;
+  if (!t->pt_dev) {
+    if (cudaMalloc(&t->pt_dev, 13 * n * rb) != cudaSuccess || cudaMallocHost(&t->pt_host, 13 * n * rb) != cudaSuccess) {
+      cudaGetLastError();
+      fail(EINSPLINE_GB300_ENOMEM, "%s: scratch allocation failed", fn);
+      return;
+    }
+  }
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  fill_eval_geometry(t, a);
+  a.pos = nullptr;
+  a.inl[0] = x; a.inl[1] = y; a.inl[2] = z;
+  a.rule = 0;
+  a.layout = 1;
+  a.npts = 1;
+  a.vals = t->pt_dev;
+  a.grads = (char *)t->pt_dev + n * rb;
+  a.hess = (char *)t->pt_dev + 4 * n * rb;
+  const int VW = elems_per_thread(t);
+  int tx = ((int)((n + VW - 1) / VW) + 31) / 32 * 32;
+  if (tx > 256) tx = 256;
+  if (launch_eval(t, a, vgh, t->stream, tx, 1, 1)) return;
+  if (cudaMemcpyAsync(t->pt_host, t->pt_dev, bytes, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
+      cudaStreamSynchronize(t->stream) != cudaSuccess) {
+    cuda_check(cudaGetLastError(), fn);
+    return;
+  }
+  memcpy(vals, t->pt_host, n * rb);
+  if (vgh) {
+    memcpy(grads, (char *)t->pt_host + n * rb, 3 * n * rb);
+    memcpy(hess, (char *)t->pt_host + 4 * n * rb, 9 * n * rb);
+  }
+}
+
+// Batched, reference GPU-entry semantics and layout, pointer-array outputs.
+template <typename CS>
+void eval_cuda(CS *c, const void *pos_d, bool pos_f64, void *const *vals_d, void *const *grads_d,
+               void *const *hess_d, int num, bool vgh, const char *fn) {
+  clear();
+  if (!c || !table_ok(c->gb300)) { fail(EINSPLINE_GB300_EINVAL, "%s: not a handle made by this library", fn); return; }
+  if (num <= 0) return;
+  Table *t = c->gb300;
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  fill_eval_geometry(t, a);
+  a.pos = pos_d;
+  a.pos_f64 = pos_f64;
+  a.rule = 1;
+  a.layout = 0;
+  a.npts = num;
+  a.vals_pp = vals_d; a.grads_pp = grads_d; a.hess_pp = hess_d;
+  int tx, ty, pb;
+  pick_tile(t, vgh, num, tx, ty, pb);
+  if (launch_eval(t, a, vgh, cudaStreamLegacy, tx, ty, pb)) return;
+  cudaError_t e = cudaStreamSynchronize(cudaStreamLegacy);
+  if (e != cudaSuccess) cuda_check(e, fn);
+}
+
+}  // namespace
+
+extern "C" {
+
+void eval_multi_UBspline_3d_s(multi_UBspline_3d_s *s, double x, double y, double z, float *vals) {
+  eval_point<multi_UBspline_3d_s, float>(s, x, y, z, vals, nullptr, nullptr, false, "eval_multi_UBspline_3d_s");
+}
+void eval_multi_UBspline_3d_s_vgh(multi_UBspline_3d_s *s, double x, double y, double z, float *vals, float *grads,
+                                  float *hess) {
+  eval_point<multi_UBspline_3d_s, float>(s, x, y, z, vals, grads, hess, true, "eval_multi_UBspline_3d_s_vgh");
+}
+void eval_multi_UBspline_3d_d(multi_UBspline_3d_d *s, double x, double y, double z, double *vals) {
+  eval_point<multi_UBspline_3d_d, double>(s, x, y, z, vals, nullptr, nullptr, false, "eval_multi_UBspline_3d_d");
+}
+void eval_multi_UBspline_3d_d_vgh(multi_UBspline_3d_d *s, double x, double y, double z, double *vals, double *grads,
+                                  double *hess) {
+  eval_point<multi_UBspline_3d_d, double>(s, x, y, z, vals, grads, hess, true, "eval_multi_UBspline_3d_d_vgh");
+}
+void eval_multi_UBspline_3d_c(multi_UBspline_3d_c *s, double x, double y, double z, complex_float *vals) {
+  eval_point<multi_UBspline_3d_c, complex_float>(s, x, y, z, vals, nullptr, nullptr, false,
+                                                 "eval_multi_UBspline_3d_c");
+}
+void eval_multi_UBspline_3d_c_vgh(multi_UBspline_3d_c *s, double x, double y, double z, complex_float *vals,
+                                  complex_float *grads, complex_float *hess) {
+  eval_point<multi_UBspline_3d_c, complex_float>(s, x, y, z, vals, grads, hess, true,
+                                                 "eval_multi_UBspline_3d_c_vgh");
+}
+void eval_multi_UBspline_3d_z(multi_UBspline_3d_z *s, double x, double y, double z, complex_double *vals) {
+  eval_point<multi_UBspline_3d_z, complex_double>(s, x, y, z, vals, nullptr, nullptr, false,
+                                                  "eval_multi_UBspline_3d_z");
+}
+void eval_multi_UBspline_3d_z_vgh(multi_UBspline_3d_z *s, double x, double y, double z, complex_double *vals,
+                                  complex_double *grads, complex_double *hess) {
+  eval_point<multi_UBspline_3d_z, complex_double>(s, x, y, z, vals, grads, hess, true,
+                                                  "eval_multi_UBspline_3d_z_vgh");
+}
+
+void eval_multi_multi_UBspline_3d_s_cuda(multi_UBspline_3d_s_cuda *c, float *pos_d, float *vals_d[], int num) {
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, nullptr, nullptr, num, false, "eval_multi_multi_UBspline_3d_s_cuda");
+}
+void eval_multi_multi_UBspline_3d_s_vgh_cuda(multi_UBspline_3d_s_cuda *c, float *pos_d, float *vals_d[],
+                                             float *grads_d[], float *hess_d[], int num) {
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, (void *const *)grads_d, (void *const *)hess_d, num, true,
+            "eval_multi_multi_UBspline_3d_s_vgh_cuda");
+}
+void eval_multi_multi_UBspline_3d_d_cuda(multi_UBspline_3d_d_cuda *c, double *pos_d, double *vals_d[], int num) {
+  eval_cuda(c, pos_d, true, (void *const *)vals_d, nullptr, nullptr, num, false, "eval_multi_multi_UBspline_3d_d_cuda");
+}
+void eval_multi_multi_UBspline_3d_d_vgh_cuda(multi_UBspline_3d_d_cuda *c, double *pos_d, double *vals_d[],
+                                             double *grads_d[], double *hess_d[], int num) {
+  eval_cuda(c, pos_d, true, (void *const *)vals_d, (void *const *)grads_d, (void *const *)hess_d, num, true,
+            "eval_multi_multi_UBspline_3d_d_vgh_cuda");
+}
+void eval_multi_multi_UBspline_3d_c_cuda(multi_UBspline_3d_c_cuda *c, float *pos_d, complex_float *vals_d[], int num) {
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, nullptr, nullptr, num, false, "eval_multi_multi_UBspline_3d_c_cuda");
+}
+void eval_multi_multi_UBspline_3d_c_vgh_cuda(multi_UBspline_3d_c_cuda *c, float *pos_d, complex_float *vals_d[],
+                                             complex_float *grads_d[], complex_float *hess_d[], int num) {
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, (void *const *)grads_d, (void *const *)hess_d, num, true,
+            "eval_multi_multi_UBspline_3d_c_vgh_cuda");
+}
+void eval_multi_multi_UBspline_3d_z_cuda(multi_UBspline_3d_z_cuda *c, double *pos_d, complex_double *vals_d[],
+                                         int num) {
+  eval_cuda(c, pos_d, true, (void *const *)vals_d, nullptr, nullptr, num, false, "eval_multi_multi_UBspline_3d_z_cuda");
+}
+void eval_multi_multi_UBspline_3d_z_vgh_cuda(multi_UBspline_3d_z_cuda *c, double *pos_d, complex_double *vals_d[],
+                                             complex_double *grads_d[], complex_double *hess_d[], int num) {
+  eval_cuda(c, pos_d, true, (void *const *)vals_d, (void *const *)grads_d, (void *const *)hess_d, num, true,
+            "eval_multi_multi_UBspline_3d_z_vgh_cuda");
+}
+
+}  // extern "C"

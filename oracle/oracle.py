@@ -1,0 +1,287 @@
+"""ctypes wrapper for the oracle (TEST INFRASTRUCTURE ONLY).
+
+The oracle is a plain-C restatement of einspline's uniform 3D multi-spline
+solve and evaluation (oracle/einspline_oracle.c).  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg may import this module,
+and only to check or to time the CPU path; the GPU library never uses it.
+
+Also wraps the reference's own CPU library (oracle/_ref/libeinspline_ref.so,
+built from the reference sources by ``make -C oracle ref``) when it exists, so
+that tests can pin the oracle against it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "build")
+REF_LIB = os.path.join(HERE, "_ref", "libeinspline_ref.so")
+
+PERIODIC, DERIV1, DERIV2, FLAT, NATURAL, ANTIPERIODIC = range(6)
+
+
+class OrcAxis(C.Structure):
+    _fields_ = [("start", C.c_double), ("end", C.c_double), ("delta", C.c_double),
+                ("delta_inv", C.c_double), ("num", C.c_int), ("ncoef", C.c_int),
+                ("lcode", C.c_int), ("rcode", C.c_int),
+                ("lval", C.c_double * 2), ("rval", C.c_double * 2)]
+
+
+class OrcDesc(C.Structure):
+    _fields_ = [("ax", OrcAxis * 3), ("num_splines", C.c_int),
+                ("xs", C.c_int64), ("ys", C.c_int64), ("zs", C.c_int64)]
+
+
+def build(fast: bool = True) -> None:
+    """Compile the oracle libraries with make (cheap; no-op when up to date)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+
+
+_libs: dict = {}
+
+
+def lib(fast: bool = False) -> C.CDLL:
+    name = "liboracle_fast.so" if fast else "liboracle.so"
+    if name not in _libs:
+        path = os.path.join(BUILD, name)
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.orc_axis_init.argtypes = [C.POINTER(OrcAxis), C.c_double, C.c_double, C.c_int, C.c_int,
+                                    C.c_int, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.orc_axis_init.restype = C.c_int
+        L.orc_find_coefs_1d_d.argtypes = [C.POINTER(OrcAxis), C.c_int, C.c_void_p, C.c_int64,
+                                          C.c_void_p, C.c_int64]
+        L.orc_set_3d_column_d.argtypes = [C.POINTER(OrcDesc), C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        for t in "sdcz":
+            f = getattr(L, "orc_eval_" + t)
+            f.argtypes = [C.POINTER(OrcDesc), C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double,
+                          C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_eval_batch.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(OrcDesc), C.c_void_p,
+                                     C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_eval_batch.restype = C.c_int
+        L.orc_max_threads.restype = C.c_int
+        _libs[name] = L
+    return _libs[name]
+
+
+def ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)
+
+
+class Table:
+    """A uniform 3D multi-spline held by the oracle: grid/BC description plus
+    a coefficient table coefs[Nx][Ny][Nz][N] (complex types: trailing axis of
+    2 for re/im).  ``kind`` is one of 's','d','c','z'."""
+
+    def __init__(self, kind, grids, bcs, num_splines):
+        # grids: 3 x (start, end, num); bcs: 3 x (lcode, rcode, lval_r, lval_i, rval_r, rval_i)
+        self.kind = kind
+        self.ncomp = 2 if kind in "cz" else 1
+        self.dtype = np.float32 if kind in "sc" else np.float64
+        self.desc = OrcDesc()
+        L = lib()
+        shape = []
+        for a in range(3):
+            st, en, num = grids[a]
+            lc, rc, *vals = bcs[a]
+            vals = list(vals) + [0.0] * (4 - len(vals))
+            n = L.orc_axis_init(C.byref(self.desc.ax[a]), st, en, num, lc, rc, *vals)
+            shape.append(n)
+        self.desc.num_splines = num_splines
+        self.N = num_splines
+        self.shape = tuple(shape)
+        self.desc.zs = num_splines
+        self.desc.ys = shape[2] * num_splines
+        self.desc.xs = shape[1] * shape[2] * num_splines
+        full = tuple(shape) + (num_splines,) + ((2,) if self.ncomp == 2 else ())
+        # FP64 solve target; for s/c the table is this rounded to float32.
+        self.coefs64 = np.zeros(full, dtype=np.float64)
+        self._coefs = None
+
+    @property
+    def M(self):
+        return tuple(self.desc.ax[a].num for a in range(3))
+
+    def set_spline(self, i: int, data: np.ndarray) -> None:
+        """FP64 solve of one spline column (set_multi_UBspline_3d_d/z); data
+        has shape (Mx,My,Mz) real or (Mx,My,Mz,2) / complex."""
+        d = np.ascontiguousarray(_as_pairs(data, self.ncomp), dtype=np.float64)
+        lib().orc_set_3d_column_d(C.byref(self.desc), self.ncomp, i, ptr(self.coefs64), ptr(d))
+        self._coefs = None
+
+    @property
+    def coefs(self) -> np.ndarray:
+        """Table in its storage precision (FP64 solve rounded once for s/c)."""
+        if self._coefs is None:
+            self._coefs = np.ascontiguousarray(self.coefs64.astype(self.dtype))
+        return self._coefs
+
+    def eval(self, pos: np.ndarray, vgh: bool = True, sem: int = 0, coefs: np.ndarray = None,
+             nthreads: int = 0, fast: bool = False):
+        """Evaluate at pos (npts,3).  sem=0: CPU-entry semantics; sem=1: the
+        reference GPU entries' cell rule.  Returns vals, grads, hess in the
+        CPU layout ([P][N], [P][N][3], [P][N][3][3], complex as a trailing 2)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        P = pos.shape[0]
+        cf = self.coefs if coefs is None else np.ascontiguousarray(coefs)
+        assert cf.dtype == self.dtype
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((P, self.N) + ext, self.dtype)
+        g = np.zeros((P, self.N, 3) + ext, self.dtype) if vgh else None
+        h = np.zeros((P, self.N, 3, 3) + ext, self.dtype) if vgh else None
+        lib(fast).orc_eval_batch(ord(self.kind), sem, int(vgh), C.byref(self.desc), ptr(cf), P,
+                                 ptr(pos), ptr(v), ptr(g), ptr(h), nthreads)
+        return v, g, h
+
+
+def _as_pairs(data, ncomp):
+    data = np.asarray(data)
+    if ncomp == 2 and np.iscomplexobj(data):
+        return np.stack([data.real, data.imag], axis=-1)
+    return data
+
+
+# --------------------------------------------------------------------------
+# The reference's own CPU library (optional: present only where the
+# reference sources were available to compile).
+# --------------------------------------------------------------------------
+class RefUgrid(C.Structure):
+    _fields_ = [("start", C.c_double), ("end", C.c_double), ("num", C.c_int),
+                ("delta", C.c_double), ("delta_inv", C.c_double)]
+
+
+class RefBC_s(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal", C.c_float), ("rVal", C.c_float)]
+
+
+class RefBC_d(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal", C.c_double), ("rVal", C.c_double)]
+
+
+class RefBC_c(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal_r", C.c_float), ("lVal_i", C.c_float),
+                ("rVal_r", C.c_float), ("rVal_i", C.c_float)]
+
+
+class RefBC_z(C.Structure):
+    _fields_ = [("lCode", C.c_int), ("rCode", C.c_int), ("lVal_r", C.c_double), ("lVal_i", C.c_double),
+                ("rVal_r", C.c_double), ("rVal_i", C.c_double)]
+
+
+def _ref_struct(bc_t):
+    class S(C.Structure):
+        _fields_ = [("spcode", C.c_int), ("tcode", C.c_int), ("coefs", C.c_void_p),
+                    ("x_stride", C.c_ssize_t), ("y_stride", C.c_ssize_t), ("z_stride", C.c_ssize_t),
+                    ("x_grid", RefUgrid), ("y_grid", RefUgrid), ("z_grid", RefUgrid),
+                    ("xBC", bc_t), ("yBC", bc_t), ("zBC", bc_t), ("num_splines", C.c_int)]
+    return S
+
+
+REF_BC = {"s": RefBC_s, "d": RefBC_d, "c": RefBC_c, "z": RefBC_z}
+REF_STRUCT = {k: _ref_struct(v) for k, v in REF_BC.items()}
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+_ref = None
+
+
+def ref_lib() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        _ref = C.CDLL(REF_LIB)
+        for t in "sdcz":
+            S = REF_STRUCT[t]
+            bc = REF_BC[t]
+            f = getattr(_ref, f"create_multi_UBspline_3d_{t}")
+            f.argtypes = [RefUgrid] * 3 + [bc] * 3 + [C.c_int]
+            f.restype = C.POINTER(S)
+            getattr(_ref, f"set_multi_UBspline_3d_{t}").argtypes = [C.POINTER(S), C.c_int, C.c_void_p]
+            getattr(_ref, f"eval_multi_UBspline_3d_{t}").argtypes = [C.POINTER(S), C.c_double, C.c_double,
+                                                                     C.c_double, C.c_void_p]
+            getattr(_ref, f"eval_multi_UBspline_3d_{t}_vgh").argtypes = [
+                C.POINTER(S), C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+        _ref.destroy_Bspline.argtypes = [C.c_void_p]
+    return _ref
+
+
+class RefSpline:
+    """A spline built by the reference's own create/set (its native solve:
+    float for s/c, double for d/z)."""
+
+    def __init__(self, kind, grids, bcs, num_splines):
+        L = ref_lib()
+        self.kind, self.N = kind, num_splines
+        self.ncomp = 2 if kind in "cz" else 1
+        self.dtype = np.float32 if kind in "sc" else np.float64
+        ug = [RefUgrid(g[0], g[1], g[2], 0.0, 0.0) for g in grids]
+        BC = REF_BC[kind]
+        bcs_c = []
+        for b in bcs:
+            lc, rc, *v = b
+            v = list(v) + [0.0] * (4 - len(v))
+            if kind in "sd":
+                bcs_c.append(BC(lc, rc, v[0], v[2]))
+            else:
+                bcs_c.append(BC(lc, rc, v[0], v[1], v[2], v[3]))
+        self.p = getattr(L, f"create_multi_UBspline_3d_{kind}")(*ug, *bcs_c, num_splines)
+        s = self.p.contents
+        self.shape = tuple(self._n(g, b) for g, b in zip(grids, bcs))
+        self.strides = (s.x_stride, s.y_stride, s.z_stride)
+
+    @staticmethod
+    def _n(g, b):
+        return g[2] + 3 if b[0] in (PERIODIC, ANTIPERIODIC) else g[2] + 2
+
+    def set_spline(self, i, data):
+        d = np.ascontiguousarray(_as_pairs(data, self.ncomp), dtype=self.dtype)
+        getattr(ref_lib(), f"set_multi_UBspline_3d_{self.kind}")(self.p, i, ptr(d))
+
+    def table(self) -> np.ndarray:
+        s = self.p.contents
+        n = self.shape[0] * s.x_stride * self.ncomp
+        buf = (C.c_float if self.dtype == np.float32 else C.c_double) * n
+        arr = np.frombuffer(buf.from_address(s.coefs), dtype=self.dtype).copy()
+        arr = arr.reshape(self.shape + (s.z_stride,) + ((2,) if self.ncomp == 2 else ()))
+        return arr[:, :, :, :self.N]
+
+    def load_table(self, coefs: np.ndarray) -> None:
+        """Overwrite the reference table with coefs (same layout) so that its
+        evaluators run on exactly the table under test."""
+        s = self.p.contents
+        n = self.shape[0] * s.x_stride * self.ncomp
+        buf = (C.c_float if self.dtype == np.float32 else C.c_double) * n
+        arr = np.frombuffer(buf.from_address(s.coefs), dtype=self.dtype)
+        arr = arr.reshape(self.shape + (s.z_stride,) + ((2,) if self.ncomp == 2 else ()))
+        arr[:, :, :, :self.N] = coefs.astype(self.dtype)
+
+    def eval(self, pos, vgh=True):
+        pos = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+        P = pos.shape[0]
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((P, self.N) + ext, self.dtype)
+        g = np.zeros((P, self.N, 3) + ext, self.dtype)
+        h = np.zeros((P, self.N, 3, 3) + ext, self.dtype)
+        L = ref_lib()
+        fv = getattr(L, f"eval_multi_UBspline_3d_{self.kind}")
+        fg = getattr(L, f"eval_multi_UBspline_3d_{self.kind}_vgh")
+        for p in range(P):
+            x, y, z = (float(c) for c in pos[p])
+            if vgh:
+                fg(self.p, x, y, z, ptr(v[p]), ptr(g[p]), ptr(h[p]))
+            else:
+                fv(self.p, x, y, z, ptr(v[p]))
+        return (v, g, h) if vgh else (v, None, None)
+
+    def __del__(self):
+        try:
+            ref_lib().destroy_Bspline(C.cast(self.p, C.c_void_p))
+        except Exception:
+            pass

@@ -1,0 +1,64 @@
+"""Shared helpers for the parity tests: the same seeded spline built by the
+GPU library and by the oracle, output-layout conversions and tolerances."""
+from __future__ import annotations
+
+import numpy as np
+
+from einspline_gb300 import api, synth
+
+# Parity tolerances, as max |gpu - oracle| / max |oracle| per quantity
+# (value, gradient, Hessian separately).  FP32 arithmetic (s/c, and the
+# 16-bit tables which compute in FP32) vs the oracle's FP32 on the same
+# table: a few ulps of the accumulated sum.  FP64 (d/z): 1e-12 relative.
+TOL = {"s": 2e-5, "c": 2e-5, "d": 1e-12, "z": 1e-12}
+
+HESS6 = [0, 1, 2, 4, 5, 8]  # (xx, xy, xz, yy, yz, zz) in a row-major 3x3
+
+
+def build_pair(orc, kind, grids, bcs, N, seed=11, storage=api.STORE_NATIVE, data=None):
+    """(gpu spline, oracle table, data): data set through set_multi_UBspline_3d_*."""
+    M = tuple(g[2] for g in grids)
+    cpx = kind in "cz"
+    dt = np.float32 if kind in "sc" else np.float64
+    if data is None:
+        data = synth.grid_data_uniform(seed, M, N, dt, complex_=cpx)
+    G = api.MultiUBspline3D(kind, grids, bcs, N, storage=storage)
+    T = orc.Table(kind, grids, bcs, N)
+    for i in range(N):
+        G.set(i, data[i])
+        T.set_spline(i, data[i].astype(np.float64))
+    G.flush()
+    return G, T, data
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.abs(b).max()
+    return float(np.abs(a - b).max() / (den if den > 0 else 1.0))
+
+
+def assert_close(got, ref, tol, what=""):
+    names = ("value", "gradient", "hessian")
+    for n, x, y in zip(names, got, ref):
+        if x is None or y is None:
+            continue
+        e = rel_err(x, y)
+        assert e <= tol, f"{what} {n}: rel err {e:.3e} > {tol:.1e}"
+
+
+def cpu_to_gpu_layout(kind, v, g, h):
+    """Oracle CPU layout -> reference GPU layout (hess [N][6]; complex
+    grads/hess [N][re,im][3|6])."""
+    if kind in "cz":
+        P, N = v.shape[:2]
+        g2 = np.moveaxis(g, -1, -2)               # [P][N][2][3]
+        hh = h.reshape(P, N, 9, 2)[:, :, HESS6, :]  # [P][N][6][2]
+        h2 = np.moveaxis(hh, -1, -2)              # [P][N][2][6]
+        return v, g2, h2
+    P, N = v.shape[:2]
+    return v, g, h.reshape(P, N, 9)[:, :, HESS6]
+
+
+def table_box(grids):
+    return [g[0] for g in grids], [g[1] for g in grids]

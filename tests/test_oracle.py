@@ -1,0 +1,83 @@
+"""The oracle against the reference: bit-exact on the committed golden
+vectors (made by the compiled reference, tests/golden/make_golden.py) and,
+where the reference sources can be compiled, against the live reference."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+def _load(path):
+    z = np.load(path)
+    kind = str(z["kind"])
+    grids = [tuple(g[:2]) + (int(g[2]),) for g in z["grids"]]
+    bcs = [tuple([int(b[0]), int(b[1])] + list(b[2:])) for b in z["bcs"]]
+    return kind, grids, bcs, int(z["num_splines"]), z
+
+
+def test_golden_present():
+    assert len(GOLDEN) == 8
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_table(orc, path):
+    kind, grids, bcs, N, z = _load(path)
+    T = orc.Table(kind, grids, bcs, N)
+    for i in range(N):
+        T.set_spline(i, z["data"][i])
+    if kind in "dz":
+        # FP64 solve: bit-identical to the reference's set_multi_UBspline_3d_d/z.
+        assert np.array_equal(T.coefs64, z["table"])
+    else:
+        # The reference solves s/c in float; the FP64 solve rounded once
+        # differs from it by float rounding only.
+        ref = z["table"].astype(np.float64)
+        rel = np.abs(T.coefs64 - ref).max() / np.abs(ref).max()
+        assert rel < 1e-6
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_eval(orc, path):
+    kind, grids, bcs, N, z = _load(path)
+    T = orc.Table(kind, grids, bcs, N)
+    table = np.ascontiguousarray(z["table"])
+    v0, _, _ = T.eval(z["pos"], vgh=False, coefs=table)
+    v, g, h = T.eval(z["pos"], vgh=True, coefs=table)
+    assert np.array_equal(v0, z["value"])
+    assert np.array_equal(v, z["vals"])
+    assert np.array_equal(g, z["grads"])
+    assert np.array_equal(h, z["hess"])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref",
+                                                    "libeinspline_ref.so")),
+                    reason="reference library not built here (make -C oracle ref)")
+@pytest.mark.parametrize("kind", "sdcz")
+def test_live_reference(orc, kind):
+    from einspline_gb300 import synth
+    P, NA, D1, D2, FL, AP = orc.PERIODIC, orc.NATURAL, orc.DERIV1, orc.DERIV2, orc.FLAT, orc.ANTIPERIODIC
+    cases = [([(0.0, 1.0, 10), (0.0, 1.0, 11), (0.0, 1.0, 12)], [(P, P)] * 3),
+             ([(0.2, 1.4, 9), (-1.0, 0.5, 7), (0.0, 3.0, 10)],
+              [(FL, D2, 0, 0, 0.7, -0.3), (AP, AP), (D1, NA, -0.4, 0.9, 0, 0)])]
+    for grids, bcs in cases:
+        N = 7
+        T = orc.Table(kind, grids, bcs, N)
+        R = orc.RefSpline(kind, grids, bcs, N)
+        data = synth.grid_data_uniform(77, T.M, N, np.float64, complex_=kind in "cz")
+        for i in range(N):
+            T.set_spline(i, data[i])
+            R.set_spline(i, data[i])
+        if kind in "dz":
+            assert np.array_equal(T.coefs64, R.table())
+        R.load_table(T.coefs)
+        pos = synth.points_uniform(5, 64, [g[0] for g in grids], [g[1] for g in grids])
+        for vgh in (False, True):
+            a = T.eval(pos, vgh=vgh)
+            b = R.eval(pos, vgh=vgh)
+            for x, y in zip(a, b):
+                if x is not None:
+                    assert np.array_equal(x, y)
