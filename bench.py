@@ -133,7 +133,7 @@ def build_tables(device_data=True):
     bcs = [(api.PERIODIC, api.PERIODIC)] * 3
     per = GRID ** 3
     tabs = {}
-    for name, st in (("f32", api.STORE_F32), ("f16", api.STORE_F16)):
+    for name, st in (("f32", api.STORE_F32), ("f16", api.STORE_F16), ("i16", api.STORE_I16)):
         tabs[name] = api.MultiUBspline3D("s", grids, bcs, NSPL, storage=st)
     chunk = 128
     buf = torch.empty((chunk, GRID, GRID, GRID), dtype=torch.float32, device="cuda")
@@ -294,6 +294,7 @@ def run_gpu(args):
     with ClockSampler(local) as clk:
         ev16, ms16, l16 = timed(tabs["f16"])
         ev32, ms32, l32 = timed(tabs["f32"])
+        evi, msi, _ = timed(tabs["i16"])
         # repeat the headline loop once more so the sampler sees sustained load
         ev16b, ms16b, _ = timed(tabs["f16"])
     ms16 = min(ms16, ms16b) if args.steps > 0 else ms16
@@ -329,19 +330,29 @@ def run_gpu(args):
         e2e = {"value": ev / el * world, "unit": UNIT, "h2d_bytes_per_step": h2d // len(hp),
                "d2h_bytes_per_step": d2h // len(hp), "path": "einspline_gb300_eval_3d_host (pinned host buffers)"}
 
-    # request latency: each walker evaluated alone, arrival-to-ready on the device
-    lat = []
+    # serving: Poisson arrivals of single-walker requests replayed natively
+    # through the request server (continuous batching, graph launches);
+    # latency = submit to results ready in device memory
+    serving = []
     if args.latency_requests > 0:
-        t = tabs["f16"]
         from einspline_gb300 import synth
-        sizes = synth.walker_sizes(4242, args.latency_requests)
-        for i, n in enumerate(sizes):
-            p = torch.from_numpy(synth.points_uniform(5000 + i, int(n))).cuda()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            t.eval(p, vgh=True, rule=0, layout=0, out=(out[0][:n], out[1][:n], out[2][:n]))
-            torch.cuda.synchronize()
-            lat.append((time.perf_counter() - t0) * 1e3)
+        srv = api.Server(tabs["f16"], max_inflight=3, max_batch_points=16384)
+        cap = rate16 / (NSPL * 272.0)  # requests/s the device sustains at the timed throughput
+        for frac in args.load:
+            n = args.latency_requests
+            sizes = synth.walker_sizes(4242, n)
+            arr = synth.poisson_arrivals(4243, n, frac * cap)
+            pts = synth.points_uniform(4244, int(sizes.sum()))
+            w = min(n, 200)
+            srv.replay(np.arange(w) * 1e-5, sizes[:w], pts[: int(sizes[:w].sum())])  # warm-up
+            lat, wall = srv.replay(arr, sizes, pts)
+            serving.append({"offered_load": frac, "rate_req_s": frac * cap, "requests": n,
+                            "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                            "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                            "evals_per_s": float(sizes.sum() * NSPL / wall)})
+        st = srv.stats()
+        srv.close()
+        serving_stats = {"batches": int(st.batches), "peak_inflight": int(st.peak_inflight)}
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
@@ -362,9 +373,12 @@ def run_gpu(args):
         "config": workload_config(),
         "fp32_table": {"value": rate32, "ms_per_step": ms32 / args.steps, "launches": l32},
         "fp16_vs_fp32": rate16 / rate32,
-        "latency_ms": ({"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                        "requests": len(lat), "mode": "one walker per launch, host clock, device idle otherwise"}
-                       if lat else None),
+        "i16_table": {"value": evi / (msi / 1e3), "ms_per_step": msi / args.steps},
+        "latency_ms": ({"p50": serving[0]["p50_ms"], "p99": serving[0]["p99_ms"],
+                        "offered_load": serving[0]["offered_load"],
+                        "mode": "request server, Poisson arrivals of 1-walker requests, submit to results ready"}
+                       if serving else None),
+        "serving": ({"sweep": serving, **serving_stats} if serving else None),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "kernel": "k_eval<F16,vgh>",
                      "bytes_per_eval": BYTES_F16,
@@ -403,6 +417,7 @@ def precision_report(tabs, npts):
     rep = {}
     for name, t in tabs.items():
         v, g, h = (x.cpu().numpy() for x in t.eval(torch.from_numpy(pos).cuda(), vgh=True, rule=0, layout=0))
+        v, g, h = v.astype(np.float64), g.astype(np.float64), h.astype(np.float64)
         q = {}
         for qn, a, b in (("value", v[:, cols], rv), ("gradient", g[:, cols], rg), ("hessian", h[:, cols], rh)):
             d = (a.astype(np.float64) - b) / np.abs(b).max()
@@ -421,7 +436,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=8)
-    ap.add_argument("--latency-requests", type=int, default=200)
+    ap.add_argument("--latency-requests", type=int, default=4000)
+    ap.add_argument("--load", type=float, nargs="*", default=[0.5, 0.9])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--error-points", type=int, default=256)
     args = ap.parse_args()

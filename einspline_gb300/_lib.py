@@ -12,8 +12,10 @@ from . import build as _build
 
 PERIODIC, DERIV1, DERIV2, FLAT, NATURAL, ANTIPERIODIC = range(6)
 SINGLE_REAL, DOUBLE_REAL, SINGLE_COMPLEX, DOUBLE_COMPLEX = range(4)
-STORE_NATIVE, STORE_F32, STORE_F16, STORE_BF16, STORE_F64 = range(5)
-STORAGE_NAMES = {STORE_NATIVE: "native", STORE_F32: "f32", STORE_F16: "f16", STORE_BF16: "bf16", STORE_F64: "f64"}
+STORE_NATIVE, STORE_F32, STORE_F16, STORE_BF16, STORE_F64, STORE_I16 = range(6)
+STORAGE_NAMES = {STORE_NATIVE: "native", STORE_F32: "f32", STORE_F16: "f16", STORE_BF16: "bf16", STORE_F64: "f64",
+                 STORE_I16: "i16"}
+I16_BIAS = 32768
 
 
 class Ugrid(C.Structure):
@@ -91,6 +93,17 @@ class TableInfo(C.Structure):
                 ("table_bytes", C.c_uint64), ("coefs", C.c_void_p), ("scale", C.c_void_p)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("vgh", C.c_int), ("pos_f64", C.c_int), ("rule", C.c_int), ("use_graphs", C.c_int),
+                ("max_inflight", C.c_int), ("max_batch_points", C.c_int), ("hbm_budget_bytes", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("released", C.c_int64),
+                ("batches", C.c_int64), ("evals", C.c_int64), ("budget_bytes", C.c_uint64),
+                ("peak_bytes_in_use", C.c_uint64), ("peak_inflight", C.c_int), ("busy_seconds", C.c_double)]
+
+
 # Every symbol the headers in include/ declare, with its ctypes signature.
 def _signatures():
     vp, i32, i64, dbl = C.c_void_p, C.c_int, C.c_int64, C.c_double
@@ -134,6 +147,16 @@ def _signatures():
     sig["einspline_gb300_autotune"] = ([vp, i64, i32], i32)
     sig["einspline_gb300_launch_count"] = ([], i64)
     sig["einspline_gb300_fill_uniform"] = ([vp, i64, i32, C.c_uint64, i64, dbl, dbl, vp], i32)
+    sig["einspline_gb300_server_create"] = ([vp, C.POINTER(ServerOpts)], vp)
+    sig["einspline_gb300_server_destroy"] = ([vp], i32)
+    sig["einspline_gb300_server_submit"] = ([vp, vp, i32], i64)
+    sig["einspline_gb300_server_wait"] = ([vp, i64, dbl], i32)
+    sig["einspline_gb300_server_result"] = ([vp, i64, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
+                                             C.POINTER(dbl)], i32)
+    sig["einspline_gb300_server_copy_result"] = ([vp, i64, vp, vp, vp], i32)
+    sig["einspline_gb300_server_release"] = ([vp, i64], i32)
+    sig["einspline_gb300_server_get_stats"] = ([vp, C.POINTER(ServerStats)], i32)
+    sig["einspline_gb300_server_replay"] = ([vp, i32, vp, vp, vp, vp, vp, C.POINTER(dbl)], i32)
     return sig
 
 

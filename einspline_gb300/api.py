@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _lib as L
 from ._lib import (ANTIPERIODIC, DERIV1, DERIV2, FLAT, NATURAL, PERIODIC, STORE_BF16, STORE_F16,  # noqa: F401
-                   STORE_F32, STORE_F64, STORE_NATIVE, EinsplineError, check)
+                   STORE_F32, STORE_F64, STORE_I16, STORE_NATIVE, EinsplineError, check)
 
 _TYPE_CODE = {"s": L.SINGLE_REAL, "d": L.DOUBLE_REAL, "c": L.SINGLE_COMPLEX, "z": L.DOUBLE_COMPLEX}
 
@@ -98,9 +98,9 @@ class MultiUBspline3D:
 
     def table_host(self):
         """(table, scales): the stored table as numpy [Nx][Ny][Nz][ncol_pad]
-        of the storage type (float16 bit patterns for BF16 are uint16)."""
+        of the storage type (bfloat16 and biased int16 patterns as uint16)."""
         ti = self.info()
-        dt = {1: np.float32, 2: np.float16, 3: np.uint16, 4: np.float64}[ti.storage]
+        dt = {1: np.float32, 2: np.float16, 3: np.uint16, 4: np.float64, 5: np.uint16}[ti.storage]
         out = np.empty((ti.nx, ti.ny, ti.nz, ti.ncol_pad), dtype=dt)
         sc = np.empty(ti.ncol, dtype=np.float32)
         _lib().einspline_gb300_copy_table(self.table, out.ctypes.data, sc.ctypes.data)
@@ -113,6 +113,8 @@ class MultiUBspline3D:
         ti = self.info()
         if ti.storage == STORE_BF16:
             t = (t.astype(np.uint32) << 16).view(np.float32)
+        elif ti.storage == STORE_I16:
+            t = t.astype(np.int32) - L.I16_BIAS
         v = t[..., :ti.ncol].astype(np.float64) * sc.astype(np.float64)
         if self.ncomp == 2:
             v = v.reshape(v.shape[:3] + (self.N, 2))
@@ -280,6 +282,85 @@ class CudaSpline:
     def __del__(self):
         try:
             self.destroy()
+        except Exception:
+            pass
+
+
+class Server:
+    """einspline_gb300_server_*: continuous batching of walker requests."""
+
+    def __init__(self, spline: MultiUBspline3D, vgh=True, pos_f64=True, rule=0, use_graphs=True,
+                 max_inflight=3, max_batch_points=16384, hbm_budget_bytes=0):
+        self.spline = spline
+        self.pos_f64 = pos_f64
+        self.vgh = vgh
+        o = L.ServerOpts(int(vgh), int(pos_f64), rule, int(use_graphs), max_inflight, max_batch_points,
+                         hbm_budget_bytes)
+        self.h = _lib().einspline_gb300_server_create(spline.table, C.byref(o))
+        check()
+        if not self.h:
+            raise EinsplineError("server create failed")
+
+    def submit(self, pos: np.ndarray) -> int:
+        pos = np.ascontiguousarray(pos, np.float64 if self.pos_f64 else np.float32)
+        rid = _lib().einspline_gb300_server_submit(self.h, C.c_void_p(pos.ctypes.data), pos.shape[0])
+        check()
+        return int(rid)
+
+    def wait(self, rid: int, timeout: float = 60.0) -> None:
+        _lib().einspline_gb300_server_wait(self.h, rid, timeout)
+        check()
+
+    def latency(self, rid: int) -> float:
+        lat = C.c_double()
+        _lib().einspline_gb300_server_result(self.h, rid, None, None, None, C.byref(lat))
+        check()
+        return lat.value
+
+    def result(self, rid: int, npts: int):
+        dt = out_dtype(self.spline.kind)
+        nr = self.spline.N * self.spline.ncomp
+        v = np.empty((npts, nr), dt)
+        g = np.empty((npts, 3 * nr), dt) if self.vgh else None
+        h = np.empty((npts, 6 * nr), dt) if self.vgh else None
+        p = lambda a: C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p(0)  # noqa: E731
+        _lib().einspline_gb300_server_copy_result(self.h, rid, p(v), p(g), p(h))
+        check()
+        return v, g, h
+
+    def release(self, rid: int) -> None:
+        _lib().einspline_gb300_server_release(self.h, rid)
+        check()
+
+    def stats(self) -> L.ServerStats:
+        s = L.ServerStats()
+        _lib().einspline_gb300_server_get_stats(self.h, C.byref(s))
+        check()
+        return s
+
+    def replay(self, arrival_s: np.ndarray, npts: np.ndarray, pos_all: np.ndarray):
+        """Open-loop native replay; returns (latencies [s], wall seconds)."""
+        n = len(npts)
+        arr = np.ascontiguousarray(arrival_s, np.float64)
+        cnt = np.ascontiguousarray(npts, np.int32)
+        off = np.ascontiguousarray(np.concatenate([[0], np.cumsum(cnt)[:-1]]), np.int64)
+        pos = np.ascontiguousarray(pos_all, np.float64 if self.pos_f64 else np.float32)
+        lat = np.zeros(n, np.float64)
+        wall = C.c_double()
+        _lib().einspline_gb300_server_replay(self.h, n, C.c_void_p(arr.ctypes.data), C.c_void_p(cnt.ctypes.data),
+                                             C.c_void_p(off.ctypes.data), C.c_void_p(pos.ctypes.data),
+                                             C.c_void_p(lat.ctypes.data), C.byref(wall))
+        check()
+        return lat, wall.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib().einspline_gb300_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

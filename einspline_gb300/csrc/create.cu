@@ -216,8 +216,8 @@ multi_UBspline_3d_z_cuda *create_multi_UBspline_3d_z_cuda(multi_UBspline_3d_z *s
 multi_UBspline_3d_s_cuda *einspline_gb300_create_3d_s_cuda_from_d(multi_UBspline_3d_d *s, int storage) {
   clear();
   if (storage == ST_NATIVE) storage = ST_F32;
-  if (storage != ST_F32 && storage != ST_F16 && storage != ST_BF16) {
-    fail(EINSPLINE_GB300_EINVAL, "storage must be F32, F16 or BF16");
+  if (storage != ST_F32 && !is16(storage)) {
+    fail(EINSPLINE_GB300_EINVAL, "storage must be F32, F16, BF16 or I16");
     return nullptr;
   }
   Table *t = table_of(s, "einspline_gb300_create_3d_s_cuda_from_d");
@@ -226,8 +226,8 @@ multi_UBspline_3d_s_cuda *einspline_gb300_create_3d_s_cuda_from_d(multi_UBspline
 multi_UBspline_3d_c_cuda *einspline_gb300_create_3d_c_cuda_from_z(multi_UBspline_3d_z *s, int storage) {
   clear();
   if (storage == ST_NATIVE) storage = ST_F32;
-  if (storage != ST_F32 && storage != ST_F16 && storage != ST_BF16) {
-    fail(EINSPLINE_GB300_EINVAL, "storage must be F32, F16 or BF16");
+  if (storage != ST_F32 && !is16(storage)) {
+    fail(EINSPLINE_GB300_EINVAL, "storage must be F32, F16, BF16 or I16");
     return nullptr;
   }
   Table *t = table_of(s, "einspline_gb300_create_3d_c_cuda_from_z");

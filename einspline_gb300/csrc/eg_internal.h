@@ -14,7 +14,11 @@ namespace eg {
 
 constexpr uint32_t kMagic = 0x45473330u;  // "EG30"
 
-enum Storage { ST_NATIVE = 0, ST_F32 = 1, ST_F16 = 2, ST_BF16 = 3, ST_F64 = 4 };
+enum Storage { ST_NATIVE = 0, ST_F32 = 1, ST_F16 = 2, ST_BF16 = 3, ST_F64 = 4, ST_I16 = 5 };
+__host__ __device__ constexpr bool is16(int st) { return st == ST_F16 || st == ST_BF16 || st == ST_I16; }
+// I16 values are stored with this bias so that a 16-bit pattern u becomes
+// the float 2^23 + u by inserting it under the exponent of 2^23.
+constexpr int kI16Bias = 32768;
 
 // ---------------------------------------------------------------- errors
 // Records a status for the calling thread; aborts when abort mode is on.
@@ -77,7 +81,7 @@ struct einspline_gb300_table {
   int64_t xs = 0, ys = 0, zs = 0;  // strides in stored reals
   size_t table_bytes = 0;
   void *coefs = nullptr;            // device
-  float *scale = nullptr;           // device, ncol_pad floats (F16/BF16)
+  float *scale = nullptr;           // device, ncol_pad floats (16-bit storage)
   bool owns = true;
 
   // queued set calls
@@ -165,6 +169,10 @@ struct EvalArgs {
 };
 
 int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb);
+// Kernel, grid, block and shared memory of a launch without launching it
+// (for graph kernel nodes); fills a.pb and a.ntiles.
+int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *grid,
+                 dim3 *block, size_t *smem);
 void fill_eval_geometry(const Table *t, EvalArgs &a);
 void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb);
 int elems_per_thread(const Table *t);

@@ -51,6 +51,20 @@ template <> struct CT<ST_BF16> {
     v[2] = __uint_as_float(x.y << 16); v[3] = __uint_as_float(x.y & 0xFFFF0000u);
   }
 };
+template <> struct CT<ST_I16> {
+  using A = float;
+  static constexpr int VW = 4, BYTES = 2;
+  // A biased 16-bit pattern u placed under the exponent of 2^23 is the float
+  // 2^23 + u; subtracting 2^23 + bias is exact and leaves the integer.
+  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
+    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(p));
+    const float off = 8388608.0f + (float)kI16Bias;
+    v[0] = __int_as_float(__byte_perm(x.x, 0x4B000000u, 0x7610)) - off;
+    v[1] = __int_as_float(__byte_perm(x.x, 0x4B000000u, 0x7632)) - off;
+    v[2] = __int_as_float(__byte_perm(x.y, 0x4B000000u, 0x7610)) - off;
+    v[3] = __int_as_float(__byte_perm(x.y, 0x4B000000u, 0x7632)) - off;
+  }
+};
 template <> struct CT<ST_F64> {
   using A = double;
   static constexpr int VW = 2, BYTES = 8;
@@ -411,11 +425,35 @@ int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty,
                          : launch_k<ST_F16, false>(a, (unsigned)blocks, block, smem, s); break;
     case ST_BF16: e = vgh ? launch_k<ST_BF16, true>(a, (unsigned)blocks, block, smem, s)
                           : launch_k<ST_BF16, false>(a, (unsigned)blocks, block, smem, s); break;
+    case ST_I16: e = vgh ? launch_k<ST_I16, true>(a, (unsigned)blocks, block, smem, s)
+                         : launch_k<ST_I16, false>(a, (unsigned)blocks, block, smem, s); break;
     default: e = vgh ? launch_k<ST_F64, true>(a, (unsigned)blocks, block, smem, s)
                      : launch_k<ST_F64, false>(a, (unsigned)blocks, block, smem, s); break;
   }
   count_launch();
   if (e != cudaSuccess) return cuda_check(e, "evaluation kernel launch");
+  return 0;
+}
+
+int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *grid,
+                 dim3 *block, size_t *smem) {
+  if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
+    return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
+  const int VW = elems_per_thread(t);
+  a.pb = pb;
+  a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
+  const int64_t blocks = ((a.npts + pb - 1) / pb) * a.ntiles;
+  if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
+  *grid = dim3((unsigned)(blocks > 0 ? blocks : 1));
+  *block = dim3(tx, ty);
+  *smem = smem_total(pb, acc_bytes(t));
+  switch (t->storage) {
+    case ST_F32: *func = vgh ? (const void *)k_eval<ST_F32, true> : (const void *)k_eval<ST_F32, false>; break;
+    case ST_F16: *func = vgh ? (const void *)k_eval<ST_F16, true> : (const void *)k_eval<ST_F16, false>; break;
+    case ST_BF16: *func = vgh ? (const void *)k_eval<ST_BF16, true> : (const void *)k_eval<ST_BF16, false>; break;
+    case ST_I16: *func = vgh ? (const void *)k_eval<ST_I16, true> : (const void *)k_eval<ST_I16, false>; break;
+    default: *func = vgh ? (const void *)k_eval<ST_F64, true> : (const void *)k_eval<ST_F64, false>; break;
+  }
   return 0;
 }
 

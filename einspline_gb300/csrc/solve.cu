@@ -292,20 +292,53 @@ __global__ void k_colmax(const double *__restrict__ W, int64_t ncells, int ncw, 
   atomicMax(colmax + c, __float_as_uint(m));
 }
 
-// Power-of-two scale per spline so that its largest |coef| lands in
-// [2^14, 2^15): scale = 2^(e-15) with max = f * 2^e, f in [0.5, 1).
-__global__ void k_scales(const unsigned int *colmax, int nslots, int ncomp, const int *slot_spline,
+// Per-spline factor for 16-bit storage, from the largest |coefficient| m:
+//   F16: m * inv just under 65504 (the largest finite half), using the whole
+//        half range;
+//   I16: m * inv = 32767, so coefficients become integers in [-32767, 32767];
+//   BF16: inv = 2^(15-e) with m = f * 2^e, f in [0.5, 1) (the exponent range
+//        of bfloat16 needs no scaling; a power of two keeps it exact).
+// The stored value is round(c * inv); evaluation multiplies by scale = 1/inv.
+__device__ __forceinline__ void choose_scale(int st, float m, float *scale, double *inv) {
+  if (!(m > 0.f)) { *scale = 1.0f; *inv = 1.0; return; }
+  double iv;
+  if (st == ST_F16) iv = (65504.0 * (1.0 - 1.0 / 1048576.0)) / (double)m;
+  else if (st == ST_I16) iv = 32767.0 / (double)m;
+  else {
+    int e = 0;
+    frexpf(m, &e);
+    iv = ldexp(1.0, 15 - e);
+  }
+  *inv = iv;
+  *scale = __double2float_rn(1.0 / iv);
+}
+
+__global__ void k_scales(int st, const unsigned int *colmax, int nslots, int ncomp, const int *slot_spline,
                          float *scale, double *inv_out) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nslots) return;
   float m = 0.f;
   for (int p = 0; p < ncomp; p++) m = fmaxf(m, __uint_as_float(colmax[s * ncomp + p]));
-  int e = 0;
-  if (m > 0.f) frexpf(m, &e);
-  const int k = (m > 0.f) ? e - 15 : 0;
+  float sc;
+  double iv;
+  choose_scale(st, m, &sc, &iv);
   for (int p = 0; p < ncomp; p++) {
-    scale[slot_spline[s] * ncomp + p] = ldexpf(1.0f, k);
-    inv_out[s * ncomp + p] = ldexp(1.0, -k);
+    scale[(slot_spline ? slot_spline[s] : s) * ncomp + p] = sc;
+    inv_out[s * ncomp + p] = iv;
+  }
+}
+
+// Rounds one FP64 coefficient to the storage type at table[o].
+template <int ST>
+__device__ __forceinline__ void store_coef(void *table, int64_t o, double w, double inv) {
+  if (ST == ST_F64) ((double *)table)[o] = w;
+  else if (ST == ST_F32) ((float *)table)[o] = __double2float_rn(w);
+  else if (ST == ST_F16) ((__half *)table)[o] = __double2half(w * inv);
+  else if (ST == ST_BF16) ((__nv_bfloat16 *)table)[o] = __double2bfloat16(w * inv);
+  else {
+    double q = rint(w * inv);
+    q = fmin(fmax(q, -32767.0), 32767.0);
+    ((unsigned short *)table)[o] = (unsigned short)((int)q + kI16Bias);
   }
 }
 
@@ -319,11 +352,7 @@ __global__ void k_store(const double *__restrict__ W, int64_t ncells, int ncw, i
   if (cell >= ncells || c >= ncw) return;
   const double w = W[cell * ncw + c];
   const int64_t tcol = (int64_t)slot_spline[c / ncomp] * ncomp + (c % ncomp);
-  const int64_t o = cell * zs + tcol;
-  if (ST == ST_F64) ((double *)table)[o] = w;
-  else if (ST == ST_F32) ((float *)table)[o] = __double2float_rn(w);
-  else if (ST == ST_F16) ((__half *)table)[o] = __double2half(w * inv[c]);
-  else ((__nv_bfloat16 *)table)[o] = __double2bfloat16(w * inv[c]);
+  store_coef<ST>(table, cell * zs + tcol, w, is16(ST) ? inv[c] : 1.0);
 }
 
 __global__ void k_fill_f32(float *p, int64_t n, float v) {
@@ -337,7 +366,7 @@ __global__ void k_fill_f32(float *p, int64_t n, float v) {
 static int resolve_storage(char kind, int storage) {
   if (kind == 'd' || kind == 'z') return (storage == ST_NATIVE || storage == ST_F64) ? ST_F64 : -1;
   if (storage == ST_NATIVE) return ST_F32;
-  if (storage == ST_F32 || storage == ST_F16 || storage == ST_BF16) return storage;
+  if (storage == ST_F32 || is16(storage)) return storage;
   return -1;
 }
 
@@ -359,7 +388,7 @@ static int alloc_storage(Table *t) {
                 t->table_bytes, cudaGetErrorString(e));
   }
   EG_CUDA(cudaMemsetAsync(t->coefs, 0, t->table_bytes, t->stream));
-  if (t->storage == ST_F16 || t->storage == ST_BF16) {
+  if (is16(t->storage)) {
     EG_CUDA(cudaMalloc(&t->scale, sizeof(float) * t->ncol_pad));
     k_fill_f32<<<(t->ncol_pad + 255) / 256, 256, 0, t->stream>>>(t->scale, t->ncol_pad, 1.0f);
     count_launch();
@@ -547,11 +576,12 @@ static int flush_locked(Table *t) {
   // 3. scales for 16-bit storage, 4. rounded store into the table columns
   const int64_t ncells = (int64_t)Nx * Ny * Nz;
   double *inv = reinterpret_cast<double *>(t->work_a);  // work_a is free again
-  if (t->storage == ST_F16 || t->storage == ST_BF16) {
+  if (is16(t->storage)) {
     EG_CUDA(cudaMemsetAsync(t->colmax, 0, ncw * sizeof(unsigned int), s));
     dim3 cg((ncw + TB - 1) / TB, (unsigned)std::min<int64_t>(ncells, 1024));
     k_colmax<<<cg, TB, 0, s>>>(t->work_w, ncells, ncw, (unsigned int *)t->colmax);
-    k_scales<<<(n + 127) / 128, 128, 0, s>>>((const unsigned int *)t->colmax, n, nc, t->slot_spline_d, t->scale, inv);
+    k_scales<<<(n + 127) / 128, 128, 0, s>>>(t->storage, (const unsigned int *)t->colmax, n, nc, t->slot_spline_d,
+                                             t->scale, inv);
     count_launch(2);
     EG_CUDA(cudaGetLastError());
   }
@@ -560,6 +590,7 @@ static int flush_locked(Table *t) {
     case ST_F64: k_store<ST_F64><<<(unsigned)sblocks, TB, 0, s>>>(t->work_w, ncells, ncw, nc, t->slot_spline_d, inv, t->coefs, t->zs); break;
     case ST_F32: k_store<ST_F32><<<(unsigned)sblocks, TB, 0, s>>>(t->work_w, ncells, ncw, nc, t->slot_spline_d, inv, t->coefs, t->zs); break;
     case ST_F16: k_store<ST_F16><<<(unsigned)sblocks, TB, 0, s>>>(t->work_w, ncells, ncw, nc, t->slot_spline_d, inv, t->coefs, t->zs); break;
+    case ST_I16: k_store<ST_I16><<<(unsigned)sblocks, TB, 0, s>>>(t->work_w, ncells, ncw, nc, t->slot_spline_d, inv, t->coefs, t->zs); break;
     default: k_store<ST_BF16><<<(unsigned)sblocks, TB, 0, s>>>(t->work_w, ncells, ncw, nc, t->slot_spline_d, inv, t->coefs, t->zs); break;
   }
   count_launch();
@@ -619,11 +650,7 @@ __global__ void k_convert(const void *__restrict__ src, int64_t szs, void *__res
   double w;
   if (SS == ST_F64) w = ((const double *)src)[cell * szs + c];
   else w = (double)((const float *)src)[cell * szs + c];
-  const int64_t o = cell * dzs + c;
-  if (DS == ST_F64) ((double *)dst)[o] = w;
-  else if (DS == ST_F32) ((float *)dst)[o] = __double2float_rn(w);
-  else if (DS == ST_F16) ((__half *)dst)[o] = __double2half(w * inv[c]);
-  else ((__nv_bfloat16 *)dst)[o] = __double2bfloat16(w * inv[c]);
+  store_coef<DS>(dst, cell * dzs + c, w, is16(DS) ? inv[c] : 1.0);
 }
 
 __global__ void k_colmax_table(const void *__restrict__ src, int src_f64, int64_t zs, int64_t ncells, int ncol,
@@ -636,17 +663,6 @@ __global__ void k_colmax_table(const void *__restrict__ src, int src_f64, int64_
     m = fmaxf(m, (float)fabs(w));
   }
   atomicMax(colmax + c, __float_as_uint(m));
-}
-
-__global__ void k_scales_all(const unsigned int *colmax, int nspl, int ncomp, float *scale, double *inv) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nspl) return;
-  float m = 0.f;
-  for (int p = 0; p < ncomp; p++) m = fmaxf(m, __uint_as_float(colmax[s * ncomp + p]));
-  int e = 0;
-  if (m > 0.f) frexpf(m, &e);
-  const int k = (m > 0.f) ? e - 15 : 0;
-  for (int p = 0; p < ncomp; p++) { scale[s * ncomp + p] = ldexpf(1.0f, k); inv[s * ncomp + p] = ldexp(1.0, -k); }
 }
 
 Table *table_clone(Table *src, int storage) {
@@ -689,11 +705,12 @@ Table *table_clone(Table *src, int storage) {
       return nullptr;
     }
     const int TB = 128, ncol = t->ncol;
-    if (t->storage == ST_F16 || t->storage == ST_BF16) {
+    if (is16(t->storage)) {
       cudaMemsetAsync(cm, 0, sizeof(unsigned int) * t->ncol_pad, t->stream);
       dim3 cg((ncol + TB - 1) / TB, (unsigned)std::min<int64_t>(ncells, 1024));
       k_colmax_table<<<cg, TB, 0, t->stream>>>(src->coefs, src->storage == ST_F64, src->zs, ncells, ncol, cm);
-      k_scales_all<<<(t->num_splines + 127) / 128, 128, 0, t->stream>>>(cm, t->num_splines, t->ncomp, t->scale, inv);
+      k_scales<<<(t->num_splines + 127) / 128, 128, 0, t->stream>>>(t->storage, cm, t->num_splines, t->ncomp,
+                                                                    nullptr, t->scale, inv);
       count_launch(2);
     }
     const int64_t blocks = ncells * ((ncol + TB - 1) / TB);
@@ -702,10 +719,12 @@ Table *table_clone(Table *src, int storage) {
     if (s64) {
       if (t->storage == ST_F32) EG_CONV(ST_F64, ST_F32);
       else if (t->storage == ST_F16) EG_CONV(ST_F64, ST_F16);
+      else if (t->storage == ST_I16) EG_CONV(ST_F64, ST_I16);
       else EG_CONV(ST_F64, ST_BF16);
     } else {
       if (t->storage == ST_F16) EG_CONV(ST_F32, ST_F16);
       else if (t->storage == ST_BF16) EG_CONV(ST_F32, ST_BF16);
+      else if (t->storage == ST_I16) EG_CONV(ST_F32, ST_I16);
       else EG_CONV(ST_F32, ST_F64);
     }
 #undef EG_CONV

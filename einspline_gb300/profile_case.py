@@ -1,0 +1,67 @@
+"""A small, self-contained launch of the vgh kernel for profiling.
+
+Builds one 64^3 x 1024-spline table (FP32, FP16 or I16 storage; 0.6-1.2 GB)
+and one batch of 64 walkers (about 17.6k points, 0.7 GB of outputs), then
+runs the evaluation `--launches` times and prints the CUDA-event time of each.
+Everything it touches is a few GB, larger than L2, so DRAM counters of one
+launch mean what they mean in the benchmark.
+
+    python -m einspline_gb300.profile_case --storage f16 --launches 3
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16", "i16"])
+    ap.add_argument("--launches", type=int, default=3)
+    ap.add_argument("--grid", type=int, default=64)
+    ap.add_argument("--splines", type=int, default=1024)
+    ap.add_argument("--walkers", type=int, default=64)
+    ap.add_argument("--vgh", type=int, default=1)
+    ap.add_argument("--tile", type=int, nargs=3, default=None)
+    ap.add_argument("--sort", type=int, default=0)
+    args = ap.parse_args()
+
+    import torch
+    from einspline_gb300 import api, synth
+    st = {"f32": api.STORE_F32, "f16": api.STORE_F16, "bf16": api.STORE_BF16, "i16": api.STORE_I16}[args.storage]
+    g = args.grid
+    T = api.MultiUBspline3D("s", [(0.0, 1.0, g)] * 3, [(api.PERIODIC, api.PERIODIC)] * 3, args.splines,
+                            storage=st)
+    buf = torch.empty((128, g, g, g), dtype=torch.float32, device="cuda")
+    for f in range(0, args.splines, 128):
+        n = min(128, args.splines - f)
+        api.fill_uniform(buf[:n], 20261203, -1.0, 1.0, offset=f * g ** 3)
+        T.set_device(f, buf[:n])
+    T.flush()
+    del buf
+    if args.tile:
+        T.set_tile(*args.tile)
+    sizes = synth.walker_sizes(777, args.walkers)
+    pos = torch.from_numpy(synth.points_uniform(778, int(sizes.sum()))).cuda()
+    P = pos.shape[0]
+    out = (torch.empty((P, args.splines), device="cuda"), torch.empty((P, args.splines, 3), device="cuda"),
+           torch.empty((P, args.splines, 6), device="cuda"))
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.launches):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        T.eval(pos, vgh=bool(args.vgh), rule=0, layout=0, sort=bool(args.sort), out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    bpe = 64 * (4 if st == api.STORE_F32 else 2) + (40 if args.vgh else 4)
+    print(json.dumps({"storage": args.storage, "points": P, "splines": args.splines, "ms": times,
+                      "tile": T.get_tile(), "bytes_per_eval": bpe,
+                      "GBps": [P * args.splines * bpe / (t * 1e-3) / 1e9 for t in times]}))
+
+
+if __name__ == "__main__":
+    main()

@@ -95,3 +95,15 @@ def poisson_arrivals(seed: int, n: int, rate_hz: float) -> np.ndarray:
     u = uniform(seed, n, 0.0, 1.0)
     gaps = -np.log1p(-u) / rate_hz
     return np.cumsum(gaps)
+
+
+def uniform_at(seed: int, idx: np.ndarray, lo: float = 0.0, hi: float = 1.0) -> np.ndarray:
+    """Elements of the uniform stream at arbitrary indices idx (int64 array)."""
+    i = np.asarray(idx, dtype=np.uint64) + np.uint64(1)
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + i * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        z = z ^ (z >> np.uint64(31))
+    u = (z >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+    return lo + (hi - lo) * u

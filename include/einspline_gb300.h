@@ -51,15 +51,21 @@ void einspline_gb300_set_abort_on_error(int enable);
 enum {
   EINSPLINE_GB300_STORE_NATIVE = 0, /* FP32 for s/c, FP64 for d/z */
   EINSPLINE_GB300_STORE_F32 = 1,
-  EINSPLINE_GB300_STORE_F16 = 2,    /* IEEE half, power-of-two scale per spline */
-  EINSPLINE_GB300_STORE_BF16 = 3,   /* bfloat16, power-of-two scale per spline  */
-  EINSPLINE_GB300_STORE_F64 = 4
+  EINSPLINE_GB300_STORE_F16 = 2,    /* IEEE half with a scale per spline        */
+  EINSPLINE_GB300_STORE_BF16 = 3,   /* bfloat16 with a power-of-two scale      */
+  EINSPLINE_GB300_STORE_F64 = 4,
+  EINSPLINE_GB300_STORE_I16 = 5     /* 16-bit fixed point with a scale per spline */
 };
 
 /* create_multi_UBspline_3d_{s,c} with a chosen table storage (s/c only:
- * NATIVE, F32, F16 or BF16).  The FP64 solve result of each spline is scaled
- * by a power of two so its largest coefficient lies in [2^14, 2^15), rounded
- * once to the storage type, and evaluation multiplies the scale back. */
+ * NATIVE, F32, F16, BF16 or I16).  The FP64 solve result of each spline is
+ * multiplied by a per-spline factor and rounded once to the storage type;
+ * evaluation multiplies the inverse back after the FP32 reduction.
+ *   F16: the largest |coefficient| maps to just under 65504 (full half range);
+ *   I16: coefficients map to integers in [-32767, 32767] (uniform step
+ *        max|c|/32767, the smallest absolute error of the 16-bit formats);
+ *   BF16: a power of two puts the largest |coefficient| in [2^14, 2^15).
+ * For complex splines the real and imaginary parts share one factor. */
 multi_UBspline_3d_s *einspline_gb300_create_3d_s(Ugrid x_grid, Ugrid y_grid, Ugrid z_grid,
                                                  BCtype_s xBC, BCtype_s yBC, BCtype_s zBC,
                                                  int num_splines, int storage);
@@ -93,7 +99,7 @@ typedef struct {
   int64_t x_stride, y_stride, z_stride; /* in stored reals */
   uint64_t table_bytes;
   const void *coefs;   /* device */
-  const float *scale;  /* device, per real column (F16/BF16), else NULL */
+  const float *scale;  /* device, per real column (16-bit storage), else NULL */
 } einspline_gb300_table_info;
 int einspline_gb300_get_table_info(einspline_gb300_table *t, einspline_gb300_table_info *out);
 /* Copy the stored table (padded layout, storage type) to host memory of
@@ -138,7 +144,67 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  * the fastest (for vgh when vgh != 0); the choice is cached per table. */
 int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh);
 
-/* Kernel launches this library issued on the calling thread so far. */
+/* --------------------------------------------------------------- serving */
+/* A request server over one table: QMC-walker-shaped requests (a set of
+ * points each) arrive at any time; a worker thread admits them while their
+ * outputs fit in a device-memory budget, packs admitted requests into
+ * batches and keeps several batches in flight on separate streams, each
+ * launched through a CUDA graph.  Requests that arrive while others are on
+ * the GPU join the next batch as slots and memory free up.  A request's
+ * outputs stay in device memory until it is released.  Every point is
+ * computed independently in a fixed order, so a request's results are
+ * bit-identical alone and in any mix. */
+typedef struct einspline_gb300_server einspline_gb300_server;
+typedef struct {
+  int vgh;                   /* 1: value+gradient+Hessian (default), 0: value */
+  int pos_f64;               /* positions are double (1) or float (0) */
+  int rule;                  /* cell rule, as einspline_gb300_eval_opts.rule */
+  int use_graphs;            /* 1: launch batches through CUDA graphs */
+  int max_inflight;          /* batches on the GPU at once (1..8), default 3 */
+  int max_batch_points;      /* points per batch, default 16384; also the
+                                largest request accepted */
+  uint64_t hbm_budget_bytes; /* device memory for request outputs; 0 = 4 GiB
+                                or half of the free memory, whichever is less */
+} einspline_gb300_server_opts;
+
+/* Output layout per request: vals [npts][N], grads [npts][N][3],
+ * hess [npts][N][6] (GPU layout; complex as float/double pairs per entry). */
+einspline_gb300_server *einspline_gb300_server_create(einspline_gb300_table *t,
+                                                      const einspline_gb300_server_opts *opts);
+int einspline_gb300_server_destroy(einspline_gb300_server *s);
+/* Queue a request (positions copied from host memory); returns its id >= 0,
+ * or -1 with the status set (ESIZE when it can never fit). */
+int64_t einspline_gb300_server_submit(einspline_gb300_server *s, const void *pos_host, int npts);
+/* Wait up to timeout_s seconds for a request; 0 when done, ETIMEOUT else. */
+int einspline_gb300_server_wait(einspline_gb300_server *s, int64_t id, double timeout_s);
+/* Device addresses of a finished request's outputs and its latency
+ * (submit to results ready, seconds). */
+int einspline_gb300_server_result(einspline_gb300_server *s, int64_t id, void **vals_d, void **grads_d,
+                                  void **hess_d, double *latency_s);
+/* Copy a finished request's outputs to host memory (any may be NULL). */
+int einspline_gb300_server_copy_result(einspline_gb300_server *s, int64_t id, void *vals_h, void *grads_h,
+                                       void *hess_h);
+/* Give a finished request's device memory back (admits waiting requests). */
+int einspline_gb300_server_release(einspline_gb300_server *s, int64_t id);
+
+typedef struct {
+  int64_t submitted, completed, released, batches;
+  int64_t evals;              /* (point, spline) pairs computed */
+  uint64_t budget_bytes, peak_bytes_in_use;
+  int peak_inflight;          /* most batches seen on the GPU at once */
+  double busy_seconds;        /* first launch to last completion */
+} einspline_gb300_server_stats;
+int einspline_gb300_server_get_stats(einspline_gb300_server *s, einspline_gb300_server_stats *out);
+
+/* Replay an open-loop arrival trace natively: request i (npts[i] points at
+ * pos_host + offsets[i] positions) is submitted at arrival_s[i] seconds after
+ * the call starts, released as soon as it completes, and its latency (submit
+ * to results ready) stored in latency_s[i].  Returns when all are done. */
+int einspline_gb300_server_replay(einspline_gb300_server *s, int nreq, const double *arrival_s,
+                                  const int *npts, const int64_t *offsets, const void *pos_host,
+                                  double *latency_s, double *wall_s);
+
+/* Kernel launches (and graph launches) this library has issued so far. */
 int64_t einspline_gb300_launch_count(void);
 
 /* Fill a device array with the splitmix64 uniform stream used by the

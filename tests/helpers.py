@@ -23,12 +23,20 @@ def build_pair(orc, kind, grids, bcs, N, seed=11, storage=api.STORE_NATIVE, data
     if data is None:
         data = synth.grid_data_uniform(seed, M, N, dt, complex_=cpx)
     G = api.MultiUBspline3D(kind, grids, bcs, N, storage=storage)
-    T = orc.Table(kind, grids, bcs, N)
+    T = orc.Table(kind, grids, oracle_bcs(kind, bcs), N)
     for i in range(N):
         G.set(i, data[i])
         T.set_spline(i, data[i].astype(np.float64))
     G.flush()
     return G, T, data
+
+
+def oracle_bcs(kind, bcs):
+    """Boundary values as the C API carries them: float for s/c
+    (BCtype_s/BCtype_c), double for d/z."""
+    if kind not in "sc":
+        return bcs
+    return [tuple(b[:2]) + tuple(float(np.float32(v)) for v in b[2:]) for b in bcs]
 
 
 def rel_err(a, b):

@@ -24,7 +24,7 @@ def torch_pos(pos, f64=True):
 def oracle_table(G, T):
     """The oracle evaluates the GPU's own stored table (dequantized for
     16-bit storage) so that only evaluation is compared here."""
-    if G.info().storage in (api.STORE_F16, api.STORE_BF16):
+    if G.info().storage in (api.STORE_F16, api.STORE_BF16, api.STORE_I16):
         v = G.table_values().astype(np.float32)
         return np.ascontiguousarray(v)
     return None
@@ -111,7 +111,7 @@ def test_edges_and_outside_points(orc, kind):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16])
+@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16, api.STORE_I16])
 def test_16bit_eval_matches_oracle_on_same_table(orc, storage):
     grids, bcs = MIXED
     G, T, _ = build_pair(orc, "s", grids, bcs, 24, seed=49, storage=storage)

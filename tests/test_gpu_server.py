@@ -1,0 +1,104 @@
+"""Request server: continuous batching with admission by device memory.
+Each request's results are bit-identical alone and in a mix of concurrent
+requests, and equal to the direct batched evaluation."""
+import numpy as np
+import pytest
+
+from einspline_gb300 import api, synth
+
+P = 0
+
+
+def make_spline(kind="s", N=96, M=20, storage=api.STORE_NATIVE):
+    grids = [(0.0, 1.0, M)] * 3
+    G = api.MultiUBspline3D(kind, grids, [(P, P)] * 3, N, storage=storage)
+    data = synth.grid_data_uniform(61, (M, M, M), N, np.float32 if kind in "sc" else np.float64,
+                                   complex_=kind in "cz")
+    for i in range(N):
+        G.set(i, data[i])
+    G.flush()
+    return G
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_alone_equals_in_mix(use_graphs):
+    import torch
+    G = make_spline()
+    S = api.Server(G, use_graphs=use_graphs, max_inflight=3, max_batch_points=2048)
+    probe = synth.points_uniform(62, 300)
+    rid = S.submit(probe)
+    S.wait(rid)
+    alone = S.result(rid, 300)
+    S.release(rid)
+    # the same request in the middle of 120 uneven concurrent requests
+    sizes = synth.walker_sizes(63, 120)
+    others = [synth.points_uniform(64 + i, int(n)) for i, n in enumerate(sizes)]
+    ids = []
+    for i, p in enumerate(others):
+        ids.append((S.submit(p), p.shape[0]))
+        if i == 60:
+            mid = S.submit(probe)
+    for r, n in ids:
+        S.wait(r)
+    S.wait(mid)
+    mixed = S.result(mid, 300)
+    for a, b in zip(alone, mixed):
+        assert np.array_equal(a, b)
+    # and equal to the direct evaluation of the same points
+    direct = G.eval(torch.from_numpy(probe).cuda(), rule=0, layout=0)
+    assert np.array_equal(direct[0].cpu().numpy(), alone[0])
+    assert np.array_equal(direct[1].cpu().numpy().reshape(300, -1), alone[1])
+    assert np.array_equal(direct[2].cpu().numpy().reshape(300, -1), alone[2])
+    # every other request also matches its direct evaluation
+    for (r, n), p in list(zip(ids, others))[::17]:
+        got = S.result(r, n)
+        d = G.eval(torch.from_numpy(p).cuda(), rule=0, layout=0)[0].cpu().numpy()
+        assert np.array_equal(got[0], d)
+    st = S.stats()
+    assert st.completed == 122 and st.batches >= 2
+    S.close()
+
+
+@pytest.mark.gpu
+def test_admission_waits_for_memory_and_bounded_waits():
+    G = make_spline(N=64, M=16)
+    per_req = 100 * 64 * 10 * 4  # outputs of a 100-point request
+    S = api.Server(G, max_inflight=2, max_batch_points=4096, hbm_budget_bytes=3 * per_req + 4096)
+    pts = [synth.points_uniform(70 + i, 100) for i in range(8)]
+    ids = [S.submit(p) for p in pts]
+    S.wait(ids[0])
+    S.wait(ids[2])
+    # the budget holds three requests: the fourth cannot be admitted yet
+    with pytest.raises(api.EinsplineError, match="not done"):
+        S.wait(ids[3], timeout=0.3)
+    for r in ids[:3]:
+        S.release(r)
+    for r in ids[3:]:
+        S.wait(r)
+        S.release(r)
+    st = S.stats()
+    assert st.peak_bytes_in_use <= st.budget_bytes
+    assert st.completed == 8 and st.released == 8
+    # refusals are status codes, not aborts
+    with pytest.raises(api.EinsplineError, match="exceed"):
+        S.submit(synth.points_uniform(80, 5000))
+    with pytest.raises(api.EinsplineError, match="unknown"):
+        S.release(123456)
+    S.close()
+
+
+@pytest.mark.gpu
+def test_replay_poisson_trace():
+    G = make_spline(N=128, M=24, storage=api.STORE_F16)
+    S = api.Server(G, max_inflight=3, max_batch_points=8192)
+    n = 300
+    sizes = synth.walker_sizes(90, n)
+    arr = synth.poisson_arrivals(91, n, 3000.0)
+    pos = synth.points_uniform(92, int(sizes.sum()))
+    lat, wall = S.replay(arr, sizes, pos)
+    assert (lat > 0).all()
+    assert wall >= arr[-1]
+    st = S.stats()
+    assert st.completed == n and st.released == n
+    S.close()

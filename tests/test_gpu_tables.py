@@ -3,7 +3,7 @@
 FP64 tables (d, z) must be bit-identical to the oracle's FP64 solve, which
 is itself bit-identical to the reference's set_multi_UBspline_3d_d/z.  FP32
 tables (s, c) must equal that FP64 solve rounded once to float.  16-bit tables
-must be the FP64 solve scaled by a power of two per spline and rounded once.
+must be the FP64 solve times a per-spline factor, rounded once.
 """
 import os
 
@@ -93,31 +93,41 @@ def test_bulk_device_set_equals_host_set(orc, kind):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16])
+@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16, api.STORE_I16])
 @pytest.mark.parametrize("kind", "sc")
 def test_16bit_tables_are_scaled_fp64_solve(orc, kind, storage):
+    """Each stored value is round(c * inv) of the FP64 coefficient c, with the
+    per-spline factor inv chosen from the spline's largest |c| (shared by re/im)."""
     grids, bcs = CASES[0][1], CASES[0][2]
     N = 11
     G, T, _ = build_pair(orc, kind, grids, bcs, N, seed=21, storage=storage)
     raw, sc = G.table_host()
     ti = G.info()
-    # scales: powers of two, shared by re/im, largest |coef|/scale in [2^14, 2^15)
-    assert np.all(np.log2(sc) == np.round(np.log2(sc)))
     ref = T.coefs64.reshape(T.coefs64.shape[:3] + (-1,))
-    mx = np.abs(ref).max(axis=(0, 1, 2))
+    m = np.abs(ref).max(axis=(0, 1, 2)).astype(np.float32).astype(np.float64)
     if kind == "c":
-        mx = np.repeat(np.maximum(mx[0::2], mx[1::2]), 2)
+        m = np.repeat(np.maximum(m[0::2], m[1::2]), 2)
         assert np.array_equal(sc[0::2], sc[1::2])
-    q = mx / sc
-    assert np.all((q >= 2 ** 14) & (q < 2 ** 15))
-    # each stored value is the scaled FP64 coefficient rounded once
-    scaled = ref / sc
     if storage == api.STORE_F16:
-        assert np.array_equal(raw[..., :ti.ncol], scaled.astype(np.float16))
+        inv = (65504.0 * (1.0 - 2.0 ** -20)) / m
+    elif storage == api.STORE_I16:
+        inv = 32767.0 / m
+    else:
+        e = np.frexp(m)[1]
+        inv = np.ldexp(1.0, 15 - e)
+    assert np.array_equal(sc, (1.0 / inv).astype(np.float32))
+    scaled = ref * inv
+    got = raw[..., :ti.ncol]
+    if storage == api.STORE_F16:
+        assert np.array_equal(got, scaled.astype(np.float16))
+        assert np.abs(got.astype(np.float64)).max() <= 65504
+    elif storage == api.STORE_I16:
+        q = np.clip(np.rint(scaled), -32767, 32767).astype(np.int64) + 32768
+        assert np.array_equal(got.astype(np.int64), q)
     else:
         import torch
         expect = torch.from_numpy(scaled).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16)
-        assert np.array_equal(raw[..., :ti.ncol], expect)
+        assert np.array_equal(got, expect)
 
 
 @pytest.mark.gpu
