@@ -420,11 +420,13 @@ def precision_report(tabs, npts):
         v, g, h = v.astype(np.float64), g.astype(np.float64), h.astype(np.float64)
         q = {}
         for qn, a, b in (("value", v[:, cols], rv), ("gradient", g[:, cols], rg), ("hessian", h[:, cols], rh)):
-            d = (a.astype(np.float64) - b) / np.abs(b).max()
-            q[qn] = {"max": float(np.abs(d).max()), "rms": float(np.sqrt((d ** 2).mean()))}
+            d = a.astype(np.float64) - b
+            q[qn] = {"max": float(np.abs(d).max() / np.abs(b).max()),
+                     "rms": float(np.sqrt((d ** 2).mean()) / np.abs(b).max()),
+                     "rel_l2": float(np.sqrt((d ** 2).sum() / (b ** 2).sum()))}
         rep[name] = q
     rep["note"] = (f"{npts} points x {len(cols)} sampled splines vs eval_multi_UBspline_3d_d on the FP64 table; "
-                   "errors relative to max |quantity|")
+                   "max and rms of |error| / max |quantity|, and rel_l2 = ||error|| / ||quantity||")
     return rep
 
 

@@ -121,13 +121,28 @@ def test_c3_complex_sorted_full_size(orc):
     check_nodes(G, "c", M, N, seed, 128, F32_VS_F64)
 
 
+# Value error against FP64 per storage: (max |dv| / max |v|, ||dv|| / ||v||).
+# FP16 keeps 11 significant bits of each coefficient; the B-spline
+# coefficients of rough data are several times larger than the data, so its
+# worst case sits near 1e-3 of the largest value while its relative L2 error
+# is 3-4 times smaller.  I16 (uniform 16-bit steps) is ten times tighter.
+STORAGE_TOL = {api.STORE_F32: (2e-5, 1e-5), api.STORE_F16: (1.5e-3, 1e-3), api.STORE_I16: (2e-4, 1e-4),
+               api.STORE_BF16: (1.5e-2, 1e-2)}
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("storage,tol_v", [(api.STORE_F32, 2e-5), (api.STORE_F16, 1e-3), (api.STORE_I16, 1e-4),
-                                           (api.STORE_BF16, 1.5e-2)])
-def test_c4_serving_table_errors_vs_fp64(orc, storage, tol_v):
+@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16, api.STORE_I16, api.STORE_BF16])
+def test_c4_serving_table_errors_vs_fp64(orc, storage):
     """multi_UBspline_3d_s, 64^3, 1024 splines: FP32 and 16-bit tables
     against the FP64 solve and evaluation on sampled columns."""
     import torch
+    tol_max, tol_l2 = STORAGE_TOL[storage]
     M, N, seed = (64, 64, 64), 1024, 404
     G, grids = device_table("s", M, N, seed, storage=storage)
     pos = synth.points_uniform(405, 512)
@@ -135,12 +150,10 @@ def test_c4_serving_table_errors_vs_fp64(orc, storage, tol_v):
     cols = list(range(0, N, 128))
     T = sampled_oracle(orc, "s", grids, M, seed, cols)
     rv, rg, rh = cpu_to_gpu_layout("d", *T.eval(pos, sem=0))
-    ev = rel_err(v[:, cols], rv)
-    eg = rel_err(g[:, cols], rg)
-    eh = rel_err(h[:, cols], rh)
-    assert ev <= tol_v, ev
-    assert eg <= 4 * tol_v and eh <= 8 * tol_v, (eg, eh)
-    check_nodes(G, "s", M, N, seed, 64, max(tol_v, F32_VS_F64))
+    for name, a, b in (("value", v[:, cols], rv), ("gradient", g[:, cols], rg), ("hessian", h[:, cols], rh)):
+        assert rel_err(a, b) <= tol_max, (name, rel_err(a, b))
+        assert rel_l2(a, b) <= tol_l2, (name, rel_l2(a, b))
+    check_nodes(G, "s", M, N, seed, 64, max(tol_max, F32_VS_F64))
 
 
 @pytest.mark.gpu
