@@ -261,10 +261,10 @@ def run_gpu(args):
     for t in tabs.values():
         tune(t)
 
-    def timed(t):
+    def timed(t, sort=False):
         for k in range(args.warmup):
             P = npts[k]
-            t.eval(pos_d[k], vgh=True, rule=0, layout=0, out=(out[0][:P], out[1][:P], out[2][:P]))
+            t.eval(pos_d[k], vgh=True, rule=0, layout=0, sort=sort, out=(out[0][:P], out[1][:P], out[2][:P]))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -274,7 +274,7 @@ def run_gpu(args):
         evals = 0
         for k in range(args.warmup, nb):
             P = npts[k]
-            t.eval(pos_d[k], vgh=True, rule=0, layout=0, out=(out[0][:P], out[1][:P], out[2][:P]))
+            t.eval(pos_d[k], vgh=True, rule=0, layout=0, sort=sort, out=(out[0][:P], out[1][:P], out[2][:P]))
             evals += P * NSPL
         e1.record(stream)
         torch.cuda.synchronize()
@@ -295,6 +295,8 @@ def run_gpu(args):
         ev16, ms16, l16 = timed(tabs["f16"])
         ev32, ms32, l32 = timed(tabs["f32"])
         evi, msi, _ = timed(tabs["i16"])
+        ev16s, ms16s, l16s = timed(tabs["f16"], sort=True)
+        ev32s, ms32s, _ = timed(tabs["f32"], sort=True)
         # repeat the headline loop once more so the sampler sees sustained load
         ev16b, ms16b, _ = timed(tabs["f16"])
     ms16 = min(ms16, ms16b) if args.steps > 0 else ms16
@@ -374,6 +376,9 @@ def run_gpu(args):
         "fp32_table": {"value": rate32, "ms_per_step": ms32 / args.steps, "launches": l32},
         "fp16_vs_fp32": rate16 / rate32,
         "i16_table": {"value": evi / (msi / 1e3), "ms_per_step": msi / args.steps},
+        "cell_sorted": {"f16_value": ev16s / (ms16s / 1e3), "f32_value": ev32s / (ms32s / 1e3),
+                        "launches_per_step": l16s / max(1, args.steps),
+                        "note": "points visited in Morton order of their cells (sort kernels inside the timed region)"},
         "latency_ms": ({"p50": serving[0]["p50_ms"], "p99": serving[0]["p99_ms"],
                         "offered_load": serving[0]["offered_load"],
                         "mode": "request server, Poisson arrivals of 1-walker requests, submit to results ready"}
