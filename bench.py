@@ -236,7 +236,7 @@ def workload_config():
 
 def run_gpu(args):
     import torch
-    from einspline_gb300 import api
+    from einspline_gb300 import api, parallel
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -282,13 +282,7 @@ def run_gpu(args):
             dist.barrier()
         ms = e0.elapsed_time(e1)
         launches = api.launch_count() - n0
-        if dist:
-            tt = torch.tensor([ms], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            ms = float(tt.item())
-            ev = torch.tensor([float(evals)], device="cuda")
-            dist.all_reduce(ev)
-            evals = float(ev.item())
+        ms, evals = parallel.aggregate(ms, float(evals), device="cuda")
         return evals, ms, launches
 
     with ClockSampler(local) as clk:

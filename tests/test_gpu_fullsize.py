@@ -124,9 +124,10 @@ def test_c3_complex_sorted_full_size(orc):
 # Value error against FP64 per storage: (max |dv| / max |v|, ||dv|| / ||v||).
 # FP16 keeps 11 significant bits of each coefficient; the B-spline
 # coefficients of rough data are several times larger than the data, so its
-# worst case sits near 1e-3 of the largest value while its relative L2 error
+# worst case sits near 1e-3 of the largest value (bounded by 2.44e-4 times the
+# largest coefficient, up to 2e-3 of the largest value) while its relative L2 error
 # is 3-4 times smaller.  I16 (uniform 16-bit steps) is ten times tighter.
-STORAGE_TOL = {api.STORE_F32: (2e-5, 1e-5), api.STORE_F16: (1.5e-3, 1e-3), api.STORE_I16: (2e-4, 1e-4),
+STORAGE_TOL = {api.STORE_F32: (2e-5, 1e-5), api.STORE_F16: (2e-3, 1e-3), api.STORE_I16: (2e-4, 1e-4),
                api.STORE_BF16: (1.5e-2, 1e-2)}
 
 
