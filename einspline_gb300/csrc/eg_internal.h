@@ -179,5 +179,7 @@ int elems_per_thread(const Table *t);
 
 // sorting
 int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s);
+// Morton key of each point's cell and its index (defined in api_ext.cu).
+__global__ void k_cell_keys(const EvalArgs a, uint64_t *keys, int *idx);
 
 }  // namespace eg

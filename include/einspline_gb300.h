@@ -136,6 +136,23 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
                                  int64_t npts, const void *pos_h, void *vals_h, void *grads_h,
                                  void *hess_h);
 
+/* Cell-sorted evaluation (as einspline_gb300_eval_3d with opts->sort = 1,
+ * whose sort scratch is allocated with cudaMalloc) that allocates nothing.
+ * No counterpart in the reference.  For callers that cannot let a library
+ * allocate device memory while they run -- a driver whose pool allocator owns
+ * the device's memory, or code that must not trigger the device-wide
+ * synchronisation cudaMalloc/cudaFree may cause.  The sort scratch is a fixed
+ * 10 MiB file-scope device array that every GPU loading the library holds
+ * until the process exits; npts above 262,144 is refused with ESIZE.  The
+ * first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress), so make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (different streams or
+ * threads without ordering between them) race and must be serialised.
+ * Results are bit-identical to einspline_gb300_eval_3d with sorting. */
+int einspline_gb300_eval_3d_sorted_noalloc(einspline_gb300_table *t, const einspline_gb300_eval_opts *opts,
+                                           int64_t npts, const void *pos_d, void *vals_d, void *grads_d,
+                                           void *hess_d, void *stream);
+
 /* Launch shape: tx threads along the spline axis (multiple of 32), ty point
  * lanes per block, pb points per block.  0,0,0 restores the default. */
 int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb);
