@@ -131,6 +131,15 @@ class MultiUBspline3D:
         check()
         return a.value, b.value, c.value
 
+    def set_prefetch(self, on: int) -> None:
+        _lib().einspline_gb300_set_prefetch(self.table, int(on))
+        check()
+
+    def get_prefetch(self) -> int:
+        r = _lib().einspline_gb300_get_prefetch(self.table)
+        check()
+        return int(r)
+
     def autotune(self, npts: int, vgh: bool = True):
         _lib().einspline_gb300_autotune(self.table, npts, int(vgh))
         check()

@@ -211,6 +211,14 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
   return 0;
 }
 
+int einspline_gb300_set_prefetch(einspline_gb300_table *t, int prefetch) {
+  clear();
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (prefetch < -1 || prefetch > 1) return fail(EINSPLINE_GB300_EINVAL, "prefetch must be -1, 0 or 1");
+  t->tile_pf = prefetch;
+  return 0;
+}
+
 int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb) {
   clear();
   if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
@@ -226,6 +234,12 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
   if (!table_ok(t) || !tx || !ty || !pb) return fail(EINSPLINE_GB300_EINVAL, "bad argument");
   pick_tile(t, true, 0, *tx, *ty, *pb);
   return 0;
+}
+
+int einspline_gb300_get_prefetch(einspline_gb300_table *t) {
+  clear();
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  return pick_prefetch(t, true);
 }
 
 int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
@@ -263,37 +277,47 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best = 1e30f;
-  int btx = 0, bty = 0, bpb = 0;
+  int btx = 0, bty = 0, bpb = 0, bpf = 0;
   const int VW = elems_per_thread(t);
-  const int need = (t->ncol + VW - 1) / VW;
-  for (int tx = 32; tx <= 256; tx *= 2) {
-    if (tx > 32 && (tx / 2) * VW >= t->ncol) break;  // wider tiles only idle threads
-    for (int ty = 1; tx * ty <= 256; ty *= 2)
-      for (int m = 1; m <= 8; m *= 2) {
-        const int pb = ty * m;
-        if (pb > 64) continue;
-        EvalArgs b = a;
-        if (launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb)) { cudaFree(buf); return einspline_gb300_last_error(); }
-        cudaEventRecord(e0, t->stream);
-        for (int r = 0; r < 3; r++) {
-          b = a;
-          launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb);
+  const int saved_pf = t->tile_pf;
+  const int v = vgh ? 1 : 0;
+  const int saved_tuned = t->tuned_tx[v];
+  t->tuned_tx[v] = 0;
+  for (int pf = 0; pf <= 1; pf++) {
+    t->tile_pf = pf;
+    for (int tx = 32; tx <= 256; tx *= 2) {
+      if (tx > 32 && (tx / 2) * VW >= t->ncol) break;  // wider tiles only idle threads
+      for (int ty = 1; tx * ty <= 256; ty *= 2)
+        for (int m = 1; m <= 8; m *= 2) {
+          const int pb = ty * m;
+          if (pb > 64) continue;
+          EvalArgs b = a;
+          if (launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb)) {
+            t->tile_pf = saved_pf;
+            t->tuned_tx[v] = saved_tuned;
+            cudaFree(buf);
+            return einspline_gb300_last_error();
+          }
+          cudaEventRecord(e0, t->stream);
+          for (int r = 0; r < 3; r++) {
+            b = a;
+            launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb);
+          }
+          cudaEventRecord(e1, t->stream);
+          cudaEventSynchronize(e1);
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (ms < best) { best = ms; btx = tx; bty = ty; bpb = pb; bpf = pf; }
         }
-        cudaEventRecord(e1, t->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) { best = ms; btx = tx; bty = ty; bpb = pb; }
-      }
+    }
   }
-  (void)need;
+  t->tile_pf = saved_pf;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaError_t e = cudaStreamSynchronize(t->stream);
   cudaFree(buf);
   if (e != cudaSuccess) return cuda_check(e, "autotune");
-  const int v = vgh ? 1 : 0;
-  t->tuned_tx[v] = btx; t->tuned_ty[v] = bty; t->tuned_pb[v] = bpb;
+  t->tuned_tx[v] = btx; t->tuned_ty[v] = bty; t->tuned_pb[v] = bpb; t->tuned_pf[v] = bpf;
   return 0;
 }
 

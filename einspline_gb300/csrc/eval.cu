@@ -372,6 +372,23 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
   }
   __syncthreads();
 
+  if (a.prefetch) {
+    // Ask L2 for every stencil row segment of this block's points at once:
+    // the bulk prefetches hold no registers, so the DRAM requests of all pb
+    // points are in flight together and the loads below mostly hit L2.
+    const int64_t c0 = (int64_t)tile * blockDim.x * VW;
+    const int64_t cn = min((int64_t)a.ncol_pad, c0 + (int64_t)blockDim.x * VW) - c0;
+    const unsigned bytes = (unsigned)(cn * CT<ST>::BYTES);
+    const char *tb = reinterpret_cast<const char *>(a.coefs) + c0 * CT<ST>::BYTES;
+    for (int q = tid; q < pn * 64; q += nthr) {
+      const int pp = q >> 6, r = q & 63;
+      const int64_t off = (int64_t)(sidx[3 * pp] + (r >> 4)) * a.xs + (int64_t)(sidx[3 * pp + 1] + ((r >> 2) & 3)) * a.ys +
+                          (int64_t)(sidx[3 * pp + 2] + (r & 3)) * a.zs;
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(tb + off * CT<ST>::BYTES), "r"(bytes)
+                   : "memory");
+    }
+  }
+
   const int col0 = (tile * blockDim.x + threadIdx.x) * VW;
   if (col0 >= a.ncol) return;
   const char *cbase = reinterpret_cast<const char *>(a.coefs) + (int64_t)col0 * CT<ST>::BYTES;
@@ -411,6 +428,7 @@ int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty,
     return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
   const int VW = elems_per_thread(t);
   a.pb = pb;
+  a.prefetch = pick_prefetch(t, vgh);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   const int64_t npg = (a.npts + pb - 1) / pb;
   const int64_t blocks = npg * a.ntiles;
@@ -441,6 +459,7 @@ int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const 
     return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
   const int VW = elems_per_thread(t);
   a.pb = pb;
+  a.prefetch = pick_prefetch(t, vgh);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   const int64_t blocks = ((a.npts + pb - 1) / pb) * a.ntiles;
   if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
@@ -454,6 +473,13 @@ int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const 
     case ST_I16: *func = vgh ? (const void *)k_eval<ST_I16, true> : (const void *)k_eval<ST_I16, false>; break;
     default: *func = vgh ? (const void *)k_eval<ST_F64, true> : (const void *)k_eval<ST_F64, false>; break;
   }
+  return 0;
+}
+
+int pick_prefetch(Table *t, bool vgh) {
+  if (t->tile_pf >= 0) return t->tile_pf;
+  const int v = vgh ? 1 : 0;
+  if (t->tuned_tx[v]) return t->tuned_pf[v];
   return 0;
 }
 

@@ -26,6 +26,8 @@ def main():
     ap.add_argument("--vgh", type=int, default=1)
     ap.add_argument("--tile", type=int, nargs=3, default=None)
     ap.add_argument("--sort", type=int, default=0)
+    ap.add_argument("--prefetch", type=int, default=-1)
+    ap.add_argument("--sweep", type=int, default=0, help="time every tile shape with and without prefetch")
     args = ap.parse_args()
 
     import torch
@@ -43,12 +45,36 @@ def main():
     del buf
     if args.tile:
         T.set_tile(*args.tile)
+    T.set_prefetch(args.prefetch)
     sizes = synth.walker_sizes(777, args.walkers)
     pos = torch.from_numpy(synth.points_uniform(778, int(sizes.sum()))).cuda()
     P = pos.shape[0]
     out = (torch.empty((P, args.splines), device="cuda"), torch.empty((P, args.splines, 3), device="cuda"),
            torch.empty((P, args.splines, 6), device="cuda"))
     torch.cuda.synchronize()
+    if args.sweep:
+        res = []
+        for pf in (0, 1):
+            T.set_prefetch(pf)
+            for tx in (32, 64, 128, 256):
+                for ty in (1, 2, 4, 8):
+                    if tx * ty > 256:
+                        continue
+                    for m in (1, 2, 4, 8):
+                        pb = ty * m
+                        T.set_tile(tx, ty, pb)
+                        T.eval(pos, vgh=bool(args.vgh), rule=0, layout=0, sort=bool(args.sort), out=out)
+                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        e0.record()
+                        for _ in range(3):
+                            T.eval(pos, vgh=bool(args.vgh), rule=0, layout=0, sort=bool(args.sort), out=out)
+                        e1.record()
+                        torch.cuda.synchronize()
+                        res.append((e0.elapsed_time(e1) / 3, pf, tx, ty, pb))
+        res.sort()
+        for r in res[:12]:
+            print(json.dumps({"ms": r[0], "prefetch": r[1], "tile": r[2:]}))
+        return
     times = []
     for _ in range(args.launches):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -138,6 +138,13 @@ def test_shapes_sorting_and_host_entry_are_bit_identical(orc, kind):
         got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
         for a, b in zip(got, base):
             assert np.array_equal(a, b), (tx, ty, pb)
+    G.set_prefetch(1)
+    for tx, ty, pb in [(32, 2, 8), (256, 1, 4)]:
+        G.set_tile(tx, ty, pb)
+        got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
+        for a, b in zip(got, base):
+            assert np.array_equal(a, b), ("prefetch", tx, ty, pb)
+    G.set_prefetch(-1)
     G.set_tile(0, 0, 0)
     srt = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0, sort=True)]
     for a, b in zip(srt, base):
