@@ -146,8 +146,8 @@ def _signatures():
     sig["einspline_gb300_set_tile"] = ([vp, i32, i32, i32], i32)
     sig["einspline_gb300_get_tile"] = ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32)
     sig["einspline_gb300_autotune"] = ([vp, i64, i32], i32)
-    sig["einspline_gb300_set_prefetch"] = ([vp, i32], i32)
-    sig["einspline_gb300_get_prefetch"] = ([vp], i32)
+    sig["einspline_gb300_set_load_mode"] = ([vp, i32], i32)
+    sig["einspline_gb300_get_load_mode"] = ([vp], i32)
     sig["einspline_gb300_launch_count"] = ([], i64)
     sig["einspline_gb300_fill_uniform"] = ([vp, i64, i32, C.c_uint64, i64, dbl, dbl, vp], i32)
     sig["einspline_gb300_server_create"] = ([vp, C.POINTER(ServerOpts)], vp)

@@ -131,12 +131,13 @@ class MultiUBspline3D:
         check()
         return a.value, b.value, c.value
 
-    def set_prefetch(self, on: int) -> None:
-        _lib().einspline_gb300_set_prefetch(self.table, int(on))
+    def set_load_mode(self, mode: int) -> None:
+        """0 direct loads, 1 L2 bulk prefetch, 2 shared-memory async pipeline, -1 autotuned."""
+        _lib().einspline_gb300_set_load_mode(self.table, int(mode))
         check()
 
-    def get_prefetch(self) -> int:
-        r = _lib().einspline_gb300_get_prefetch(self.table)
+    def get_load_mode(self) -> int:
+        r = _lib().einspline_gb300_get_load_mode(self.table)
         check()
         return int(r)
 

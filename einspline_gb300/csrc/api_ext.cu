@@ -211,11 +211,11 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
   return 0;
 }
 
-int einspline_gb300_set_prefetch(einspline_gb300_table *t, int prefetch) {
+int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode) {
   clear();
   if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
-  if (prefetch < -1 || prefetch > 1) return fail(EINSPLINE_GB300_EINVAL, "prefetch must be -1, 0 or 1");
-  t->tile_pf = prefetch;
+  if (mode < -1 || mode > 2) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1 or 2");
+  t->tile_mode = mode;
   return 0;
 }
 
@@ -236,10 +236,10 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
   return 0;
 }
 
-int einspline_gb300_get_prefetch(einspline_gb300_table *t) {
+int einspline_gb300_get_load_mode(einspline_gb300_table *t) {
   clear();
   if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
-  return pick_prefetch(t, true);
+  return pick_mode(t, true);
 }
 
 int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
@@ -279,21 +279,22 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
   float best = 1e30f;
   int btx = 0, bty = 0, bpb = 0, bpf = 0;
   const int VW = elems_per_thread(t);
-  const int saved_pf = t->tile_pf;
+  const int saved_pf = t->tile_mode;
   const int v = vgh ? 1 : 0;
   const int saved_tuned = t->tuned_tx[v];
   t->tuned_tx[v] = 0;
-  for (int pf = 0; pf <= 1; pf++) {
-    t->tile_pf = pf;
+  const int nmodes = t->storage == ST_F64 ? 2 : 3;
+  for (int pf = 0; pf < nmodes; pf++) {
+    t->tile_mode = pf;
     for (int tx = 32; tx <= 256; tx *= 2) {
       if (tx > 32 && (tx / 2) * VW >= t->ncol) break;  // wider tiles only idle threads
-      for (int ty = 1; tx * ty <= 256; ty *= 2)
+      for (int ty = 1; tx * ty <= 256 && (pf < 2 || ty == 1); ty *= 2)
         for (int m = 1; m <= 8; m *= 2) {
           const int pb = ty * m;
           if (pb > 64) continue;
           EvalArgs b = a;
           if (launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb)) {
-            t->tile_pf = saved_pf;
+            t->tile_mode = saved_pf;
             t->tuned_tx[v] = saved_tuned;
             cudaFree(buf);
             return einspline_gb300_last_error();
@@ -311,13 +312,13 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
         }
     }
   }
-  t->tile_pf = saved_pf;
+  t->tile_mode = saved_pf;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaError_t e = cudaStreamSynchronize(t->stream);
   cudaFree(buf);
   if (e != cudaSuccess) return cuda_check(e, "autotune");
-  t->tuned_tx[v] = btx; t->tuned_ty[v] = bty; t->tuned_pb[v] = bpb; t->tuned_pf[v] = bpf;
+  t->tuned_tx[v] = btx; t->tuned_ty[v] = bty; t->tuned_pb[v] = bpb; t->tuned_mode[v] = bpf;
   return 0;
 }
 

@@ -113,9 +113,9 @@ struct einspline_gb300_table {
   void *sort_dev = nullptr;
   size_t sort_bytes = 0;
 
-  // launch shape (pf: L2 bulk prefetch of the block's rows)
-  int tile_tx = 0, tile_ty = 0, tile_pb = 0, tile_pf = -1;
-  int tuned_tx[2] = {0, 0}, tuned_ty[2] = {0, 0}, tuned_pb[2] = {0, 0}, tuned_pf[2] = {0, 0};
+  // launch shape and load mode (-1: not forced)
+  int tile_tx = 0, tile_ty = 0, tile_pb = 0, tile_mode = -1;
+  int tuned_tx[2] = {0, 0}, tuned_ty[2] = {0, 0}, tuned_pb[2] = {0, 0}, tuned_mode[2] = {0, 0};
 };
 
 namespace eg {
@@ -166,7 +166,8 @@ struct EvalArgs {
   int is_complex;
   int ntiles;                 // column tiles per point group
   int pb;                     // points per block
-  int prefetch;               // 1: bulk-prefetch the block's stencil rows into L2 first
+  int mode;                   // load mode: 0 direct loads, 1 L2 bulk prefetch first,
+                              // 2 shared-memory pipeline of async copies
 };
 
 int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb);
@@ -176,8 +177,8 @@ int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const 
                  dim3 *block, size_t *smem);
 void fill_eval_geometry(const Table *t, EvalArgs &a);
 void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb);
-// Whether launches on this table prefetch stencil rows into L2.
-int pick_prefetch(Table *t, bool vgh);
+// Load mode of launches on this table (see EvalArgs::mode).
+int pick_mode(Table *t, bool vgh);
 int elems_per_thread(const Table *t);
 
 // sorting

@@ -23,20 +23,22 @@
 namespace eg {
 
 // ------------------------------------------------------------ coefficient types
+// Raw is what one thread reads per stencil row (VW stored reals); decode
+// turns it into VW accumulator values.
 template <int ST> struct CT;
 template <> struct CT<ST_F32> {
   using A = float;
+  using Raw = float4;
   static constexpr int VW = 4, BYTES = 4;
-  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
-    const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
     v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
   }
 };
 template <> struct CT<ST_F16> {
   using A = float;
+  using Raw = uint2;
   static constexpr int VW = 4, BYTES = 2;
-  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
-    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(p));
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
     const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&x.x));
     const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&x.y));
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
@@ -44,20 +46,20 @@ template <> struct CT<ST_F16> {
 };
 template <> struct CT<ST_BF16> {
   using A = float;
+  using Raw = uint2;
   static constexpr int VW = 4, BYTES = 2;
-  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
-    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(p));
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
     v[0] = __uint_as_float(x.x << 16); v[1] = __uint_as_float(x.x & 0xFFFF0000u);
     v[2] = __uint_as_float(x.y << 16); v[3] = __uint_as_float(x.y & 0xFFFF0000u);
   }
 };
 template <> struct CT<ST_I16> {
   using A = float;
+  using Raw = uint2;
   static constexpr int VW = 4, BYTES = 2;
   // A biased 16-bit pattern u placed under the exponent of 2^23 is the float
   // 2^23 + u; subtracting 2^23 + bias is exact and leaves the integer.
-  __device__ static __forceinline__ void load(const char *p, float (&v)[4]) {
-    const uint2 x = __ldg(reinterpret_cast<const uint2 *>(p));
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
     const float off = 8388608.0f + (float)kI16Bias;
     v[0] = __int_as_float(__byte_perm(x.x, 0x4B000000u, 0x7610)) - off;
     v[1] = __int_as_float(__byte_perm(x.x, 0x4B000000u, 0x7632)) - off;
@@ -67,12 +69,15 @@ template <> struct CT<ST_I16> {
 };
 template <> struct CT<ST_F64> {
   using A = double;
+  using Raw = double2;
   static constexpr int VW = 2, BYTES = 8;
-  __device__ static __forceinline__ void load(const char *p, double (&v)[2]) {
-    const double2 x = __ldg(reinterpret_cast<const double2 *>(p));
-    v[0] = x.x; v[1] = x.y;
-  }
+  __device__ static __forceinline__ void decode(const Raw &x, double (&v)[2]) { v[0] = x.x; v[1] = x.y; }
 };
+
+template <int ST>
+__device__ __forceinline__ void load_row(const char *p, typename CT<ST>::A (&v)[CT<ST>::VW]) {
+  CT<ST>::decode(__ldg(reinterpret_cast<const typename CT<ST>::Raw *>(p)), v);
+}
 
 int elems_per_thread(const Table *t) { return t->storage == ST_F64 ? 2 : 4; }
 static int acc_bytes(const Table *t) { return t->storage == ST_F64 ? 8 : 4; }
@@ -148,74 +153,96 @@ __device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &
 // Separable reduction of the 4x4x4 stencil for VW columns.
 // w: [0..11] x weights, [12..23] y weights, [24..35] z weights.
 // o: v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz.
-template <int ST, bool VGH>
-__device__ __forceinline__ void contract(const char *base, int64_t xsb, int64_t ysb, int64_t zsb,
-                                         const typename CT<ST>::A *w, typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
+// One x-plane i: rows (i, j, k) come from row(j, k, c); z first, then y,
+// then this plane's x terms are added to o.
+template <int ST, bool VGH, typename RowFn>
+__device__ __forceinline__ void reduce_plane(int i, const typename CT<ST>::A *w,
+                                             const typename CT<ST>::A (&wz)[3][4], RowFn row,
+                                             typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
   using A = typename CT<ST>::A;
   constexpr int VW = CT<ST>::VW;
+  A y[6][VW];
+#pragma unroll
+  for (int q = 0; q < 6; q++)
+#pragma unroll
+    for (int e = 0; e < VW; e++) y[q][e] = A(0);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    A c[4][VW];
+#pragma unroll
+    for (int k = 0; k < 4; k++) row(j, k, c[k]);
+    const A by = w[12 + j], dby = w[16 + j], d2by = w[20 + j];
+#pragma unroll
+    for (int e = 0; e < VW; e++) {
+      A z0 = c[0][e] * wz[0][0];
+      z0 = fmaT(c[1][e], wz[0][1], z0);
+      z0 = fmaT(c[2][e], wz[0][2], z0);
+      z0 = fmaT(c[3][e], wz[0][3], z0);
+      y[0][e] = fmaT(by, z0, y[0][e]);
+      if (VGH) {
+        A z1 = c[0][e] * wz[1][0];
+        z1 = fmaT(c[1][e], wz[1][1], z1);
+        z1 = fmaT(c[2][e], wz[1][2], z1);
+        z1 = fmaT(c[3][e], wz[1][3], z1);
+        A z2 = c[0][e] * wz[2][0];
+        z2 = fmaT(c[1][e], wz[2][1], z2);
+        z2 = fmaT(c[2][e], wz[2][2], z2);
+        z2 = fmaT(c[3][e], wz[2][3], z2);
+        y[1][e] = fmaT(dby, z0, y[1][e]);
+        y[2][e] = fmaT(d2by, z0, y[2][e]);
+        y[3][e] = fmaT(by, z1, y[3][e]);
+        y[4][e] = fmaT(dby, z1, y[4][e]);
+        y[5][e] = fmaT(by, z2, y[5][e]);
+      }
+    }
+  }
+  const A ax = w[i], dax = w[4 + i], d2ax = w[8 + i];
+#pragma unroll
+  for (int e = 0; e < VW; e++) {
+    o[0][e] = fmaT(ax, y[0][e], o[0][e]);
+    if (VGH) {
+      o[1][e] = fmaT(dax, y[0][e], o[1][e]);
+      o[2][e] = fmaT(ax, y[1][e], o[2][e]);
+      o[3][e] = fmaT(ax, y[3][e], o[3][e]);
+      o[4][e] = fmaT(d2ax, y[0][e], o[4][e]);
+      o[5][e] = fmaT(dax, y[1][e], o[5][e]);
+      o[6][e] = fmaT(dax, y[3][e], o[6][e]);
+      o[7][e] = fmaT(ax, y[2][e], o[7][e]);
+      o[8][e] = fmaT(ax, y[4][e], o[8][e]);
+      o[9][e] = fmaT(ax, y[5][e], o[9][e]);
+    }
+  }
+}
+
+template <int ST>
+__device__ __forceinline__ void zero_out(typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
 #pragma unroll
   for (int q = 0; q < 10; q++)
 #pragma unroll
-    for (int e = 0; e < VW; e++) o[q][e] = A(0);
-  A wz[3][4];
+    for (int e = 0; e < CT<ST>::VW; e++) o[q][e] = typename CT<ST>::A(0);
+}
+
+template <int ST>
+__device__ __forceinline__ void z_weights(const typename CT<ST>::A *w, typename CT<ST>::A (&wz)[3][4]) {
 #pragma unroll
   for (int d = 0; d < 3; d++)
 #pragma unroll
     for (int k = 0; k < 4; k++) wz[d][k] = w[24 + 4 * d + k];
+}
+
+// All four planes, rows read straight from global memory.
+template <int ST, bool VGH>
+__device__ __forceinline__ void contract(const char *base, int64_t xsb, int64_t ysb, int64_t zsb,
+                                         const typename CT<ST>::A *w, typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
+  using A = typename CT<ST>::A;
+  zero_out<ST>(o);
+  A wz[3][4];
+  z_weights<ST>(w, wz);
 #pragma unroll 1
   for (int i = 0; i < 4; i++) {
-    A y[6][VW];
-#pragma unroll
-    for (int q = 0; q < 6; q++)
-#pragma unroll
-      for (int e = 0; e < VW; e++) y[q][e] = A(0);
     const char *plane = base + i * xsb;
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      A c[4][VW];
-#pragma unroll
-      for (int k = 0; k < 4; k++) CT<ST>::load(plane + j * ysb + k * zsb, c[k]);
-      const A by = w[12 + j], dby = w[16 + j], d2by = w[20 + j];
-#pragma unroll
-      for (int e = 0; e < VW; e++) {
-        A z0 = c[0][e] * wz[0][0];
-        z0 = fmaT(c[1][e], wz[0][1], z0);
-        z0 = fmaT(c[2][e], wz[0][2], z0);
-        z0 = fmaT(c[3][e], wz[0][3], z0);
-        y[0][e] = fmaT(by, z0, y[0][e]);
-        if (VGH) {
-          A z1 = c[0][e] * wz[1][0];
-          z1 = fmaT(c[1][e], wz[1][1], z1);
-          z1 = fmaT(c[2][e], wz[1][2], z1);
-          z1 = fmaT(c[3][e], wz[1][3], z1);
-          A z2 = c[0][e] * wz[2][0];
-          z2 = fmaT(c[1][e], wz[2][1], z2);
-          z2 = fmaT(c[2][e], wz[2][2], z2);
-          z2 = fmaT(c[3][e], wz[2][3], z2);
-          y[1][e] = fmaT(dby, z0, y[1][e]);
-          y[2][e] = fmaT(d2by, z0, y[2][e]);
-          y[3][e] = fmaT(by, z1, y[3][e]);
-          y[4][e] = fmaT(dby, z1, y[4][e]);
-          y[5][e] = fmaT(by, z2, y[5][e]);
-        }
-      }
-    }
-    const A ax = w[i], dax = w[4 + i], d2ax = w[8 + i];
-#pragma unroll
-    for (int e = 0; e < VW; e++) {
-      o[0][e] = fmaT(ax, y[0][e], o[0][e]);
-      if (VGH) {
-        o[1][e] = fmaT(dax, y[0][e], o[1][e]);
-        o[2][e] = fmaT(ax, y[1][e], o[2][e]);
-        o[3][e] = fmaT(ax, y[3][e], o[3][e]);
-        o[4][e] = fmaT(d2ax, y[0][e], o[4][e]);
-        o[5][e] = fmaT(dax, y[1][e], o[5][e]);
-        o[6][e] = fmaT(dax, y[3][e], o[6][e]);
-        o[7][e] = fmaT(ax, y[2][e], o[7][e]);
-        o[8][e] = fmaT(ax, y[4][e], o[8][e]);
-        o[9][e] = fmaT(ax, y[5][e], o[9][e]);
-      }
-    }
+    reduce_plane<ST, VGH>(i, w, wz, [&](int j, int k, A(&c)[CT<ST>::VW]) { load_row<ST>(plane + j * ysb + k * zsb, c); },
+                          o);
   }
 }
 
@@ -372,7 +399,7 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
   }
   __syncthreads();
 
-  if (a.prefetch) {
+  if (a.mode == 1) {
     // Ask L2 for every stencil row segment of this block's points at once:
     // the bulk prefetches hold no registers, so the DRAM requests of all pb
     // points are in flight together and the loads below mostly hit L2.
@@ -401,6 +428,107 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
   }
 }
 
+// Points' cells, weights and sources into shared memory (both kernels).
+template <typename A>
+__device__ __forceinline__ int eval_prologue(const EvalArgs &a, unsigned char *smem, int64_t p0, int tid, int nthr) {
+  A *sw = reinterpret_cast<A *>(smem);
+  int *sidx = reinterpret_cast<int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
+  int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
+  const int pn = (int)min((int64_t)a.pb, a.npts - p0);
+  for (int q = tid; q < pn * 3; q += nthr) {
+    const int pp = q / 3, ax = q - 3 * pp;
+    const int64_t src = a.perm ? (int64_t)a.perm[p0 + pp] : p0 + pp;
+    double xd;
+    if (!a.pos) xd = a.inl[ax];
+    else if (a.pos_f64) xd = reinterpret_cast<const double *>(a.pos)[3 * src + ax];
+    else xd = (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
+    int idx;
+    A t;
+    cell(a, ax, xd, idx, t);
+    bspline_weights<A>(t, sw + pp * 36 + ax * 12);
+    sidx[pp * 3 + ax] = idx;
+    if (ax == 0) ssrc[pp] = src;
+  }
+  return pn;
+}
+
+template <int RB>
+__device__ __forceinline__ void cp_async(unsigned dst, const char *src) {
+  if (RB == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int kPipeStages = 3;
+__host__ __device__ __forceinline__ size_t pipe_bytes(int nthr, int rb) { return (size_t)kPipeStages * 16 * nthr * rb; }
+
+// Pipelined variant: a stage is one x-plane (16 stencil rows) of one point.
+// Each thread copies its own VW columns of the rows of stage s+2 into shared
+// memory with asynchronous copies while it reduces stage s, so the bytes in
+// flight are held in shared memory, not registers.  A thread only reads back
+// what it copied itself: the copy-group waits order it, no block barrier is
+// needed.  Same arithmetic, same order as k_eval.
+template <int ST, bool VGH>
+__global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
+  using A = typename CT<ST>::A;
+  using Raw = typename CT<ST>::Raw;
+  constexpr int VW = CT<ST>::VW;
+  constexpr int RB = (int)sizeof(Raw);
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tile = blockIdx.x % a.ntiles;
+  const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
+  const int nthr = blockDim.x;
+  const int pn = eval_prologue<A>(a, smem, p0, threadIdx.x, nthr);
+  __syncthreads();
+  const A *sw = reinterpret_cast<const A *>(smem);
+  const int *sidx = reinterpret_cast<const int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
+  const int64_t *ssrc =
+      reinterpret_cast<const int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
+  unsigned char *pipe = smem + align_up(smem_total(a.pb, sizeof(A)), 16);
+
+  const int col0 = (tile * blockDim.x + threadIdx.x) * VW;
+  if (col0 >= a.ncol) return;
+  const char *cbase = reinterpret_cast<const char *>(a.coefs) + (int64_t)col0 * CT<ST>::BYTES;
+  const int64_t xsb = a.xs * CT<ST>::BYTES, ysb = a.ys * CT<ST>::BYTES, zsb = a.zs * CT<ST>::BYTES;
+  const unsigned my = (unsigned)__cvta_generic_to_shared(pipe + (size_t)threadIdx.x * RB);
+  const unsigned row_step = (unsigned)(nthr * RB), slot_step = 16u * row_step;
+  const int S = pn * 4;
+  auto issue = [&](int st) {
+    const int pp = st >> 2, i = st & 3;
+    const char *plane = cbase + (sidx[3 * pp] + i) * xsb + sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
+    const unsigned dst = my + (unsigned)(st % kPipeStages) * slot_step;
+#pragma unroll
+    for (int r = 0; r < 16; r++) cp_async<RB>(dst + r * row_step, plane + (r >> 2) * ysb + (r & 3) * zsb);
+  };
+#pragma unroll
+  for (int st = 0; st < kPipeStages - 1; st++) {
+    if (st < S) issue(st);
+    cp_async_commit();
+  }
+  A o[10][VW];
+  zero_out<ST>(o);
+  for (int st = 0; st < S; st++) {
+    if (st + kPipeStages - 1 < S) issue(st + kPipeStages - 1);
+    cp_async_commit();
+    cp_async_wait<kPipeStages - 1>();
+    const int pp = st >> 2, i = st & 3;
+    const A *w = sw + pp * 36;
+    A wz[3][4];
+    z_weights<ST>(w, wz);
+    const unsigned char *slot = pipe + (size_t)(st % kPipeStages) * slot_step + (size_t)threadIdx.x * RB;
+    reduce_plane<ST, VGH>(
+        i, w, wz,
+        [&](int j, int k, A(&c)[VW]) { CT<ST>::decode(*reinterpret_cast<const Raw *>(slot + (j * 4 + k) * row_step), c); },
+        o);
+    if (i == 3) {
+      epilogue<ST, VGH>(a, ssrc[pp], col0, o);
+      zero_out<ST>(o);
+    }
+  }
+}
+
 void fill_eval_geometry(const Table *t, EvalArgs &a) {
   a.coefs = t->coefs;
   a.scale = t->scale;
@@ -417,24 +545,58 @@ void fill_eval_geometry(const Table *t, EvalArgs &a) {
 }
 
 template <int ST, bool VGH>
+static const void *kernel_for(int mode) {
+  return mode == 2 ? (const void *)k_eval_pipe<ST, VGH> : (const void *)k_eval<ST, VGH>;
+}
+
+template <int ST, bool VGH>
 static cudaError_t launch_k(const EvalArgs &a, unsigned grid, dim3 block, size_t smem, cudaStream_t s) {
-  k_eval<ST, VGH><<<grid, block, smem, s>>>(a);
+  if (a.mode == 2) k_eval_pipe<ST, VGH><<<grid, block, smem, s>>>(a);
+  else k_eval<ST, VGH><<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+// Kernel, block and dynamic shared memory of a launch; the pipelined kernel
+// runs one point lane (ty = 1) and needs its stage buffers raised above the
+// 48 KB default once per kernel.
+static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *block,
+                        size_t *smem) {
+  if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
+    return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
+  a.pb = pb;
+  a.mode = pick_mode(t, vgh);
+  if (a.mode == 2 && t->storage == ST_F64) a.mode = 0;  // FP64 is FMA-bound: no pipeline variant
+  const int VW = elems_per_thread(t);
+  a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
+  *smem = smem_total(pb, acc_bytes(t));
+  if (a.mode == 2) {
+    ty = 1;
+    const int rb = t->storage == ST_F32 ? 16 : 8;
+    *smem = align_up(*smem, 16) + pipe_bytes(tx, rb);
+  }
+  *block = dim3(tx, ty);
+  switch (t->storage) {
+    case ST_F32: *func = vgh ? kernel_for<ST_F32, true>(a.mode) : kernel_for<ST_F32, false>(a.mode); break;
+    case ST_F16: *func = vgh ? kernel_for<ST_F16, true>(a.mode) : kernel_for<ST_F16, false>(a.mode); break;
+    case ST_BF16: *func = vgh ? kernel_for<ST_BF16, true>(a.mode) : kernel_for<ST_BF16, false>(a.mode); break;
+    case ST_I16: *func = vgh ? kernel_for<ST_I16, true>(a.mode) : kernel_for<ST_I16, false>(a.mode); break;
+    default: *func = vgh ? kernel_for<ST_F64, true>(a.mode) : kernel_for<ST_F64, false>(a.mode); break;
+  }
+  if (*smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(*func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+    if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute(max dynamic shared memory)");
+  }
+  return 0;
 }
 
 int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb) {
   if (a.npts <= 0) return 0;
-  if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
-    return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
-  const int VW = elems_per_thread(t);
-  a.pb = pb;
-  a.prefetch = pick_prefetch(t, vgh);
-  a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
-  const int64_t npg = (a.npts + pb - 1) / pb;
-  const int64_t blocks = npg * a.ntiles;
+  const void *func;
+  dim3 block;
+  size_t smem;
+  if (int r = shape_launch(t, a, vgh, tx, ty, pb, &func, &block, &smem)) return r;
+  const int64_t blocks = ((a.npts + pb - 1) / pb) * a.ntiles;
   if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
-  const size_t smem = smem_total(pb, acc_bytes(t));
-  dim3 block(tx, ty);
   cudaError_t e;
   switch (t->storage) {
     case ST_F32: e = vgh ? launch_k<ST_F32, true>(a, (unsigned)blocks, block, smem, s)
@@ -455,31 +617,17 @@ int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty,
 
 int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *grid,
                  dim3 *block, size_t *smem) {
-  if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
-    return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
-  const int VW = elems_per_thread(t);
-  a.pb = pb;
-  a.prefetch = pick_prefetch(t, vgh);
-  a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
+  if (int r = shape_launch(t, a, vgh, tx, ty, pb, func, block, smem)) return r;
   const int64_t blocks = ((a.npts + pb - 1) / pb) * a.ntiles;
   if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
   *grid = dim3((unsigned)(blocks > 0 ? blocks : 1));
-  *block = dim3(tx, ty);
-  *smem = smem_total(pb, acc_bytes(t));
-  switch (t->storage) {
-    case ST_F32: *func = vgh ? (const void *)k_eval<ST_F32, true> : (const void *)k_eval<ST_F32, false>; break;
-    case ST_F16: *func = vgh ? (const void *)k_eval<ST_F16, true> : (const void *)k_eval<ST_F16, false>; break;
-    case ST_BF16: *func = vgh ? (const void *)k_eval<ST_BF16, true> : (const void *)k_eval<ST_BF16, false>; break;
-    case ST_I16: *func = vgh ? (const void *)k_eval<ST_I16, true> : (const void *)k_eval<ST_I16, false>; break;
-    default: *func = vgh ? (const void *)k_eval<ST_F64, true> : (const void *)k_eval<ST_F64, false>; break;
-  }
   return 0;
 }
 
-int pick_prefetch(Table *t, bool vgh) {
-  if (t->tile_pf >= 0) return t->tile_pf;
+int pick_mode(Table *t, bool vgh) {
+  if (t->tile_mode >= 0) return t->tile_mode;
   const int v = vgh ? 1 : 0;
-  if (t->tuned_tx[v]) return t->tuned_pf[v];
+  if (t->tuned_tx[v]) return t->tuned_mode[v];
   return 0;
 }
 

@@ -26,8 +26,8 @@ def main():
     ap.add_argument("--vgh", type=int, default=1)
     ap.add_argument("--tile", type=int, nargs=3, default=None)
     ap.add_argument("--sort", type=int, default=0)
-    ap.add_argument("--prefetch", type=int, default=-1)
-    ap.add_argument("--sweep", type=int, default=0, help="time every tile shape with and without prefetch")
+    ap.add_argument("--mode", type=int, default=-1, help="load mode: 0 direct, 1 L2 prefetch, 2 smem pipeline")
+    ap.add_argument("--sweep", type=int, default=0, help="time every tile shape in every load mode")
     args = ap.parse_args()
 
     import torch
@@ -45,7 +45,7 @@ def main():
     del buf
     if args.tile:
         T.set_tile(*args.tile)
-    T.set_prefetch(args.prefetch)
+    T.set_load_mode(args.mode)
     sizes = synth.walker_sizes(777, args.walkers)
     pos = torch.from_numpy(synth.points_uniform(778, int(sizes.sum()))).cuda()
     P = pos.shape[0]
@@ -54,11 +54,11 @@ def main():
     torch.cuda.synchronize()
     if args.sweep:
         res = []
-        for pf in (0, 1):
-            T.set_prefetch(pf)
+        for pf in (0, 1, 2):
+            T.set_load_mode(pf)
             for tx in (32, 64, 128, 256):
                 for ty in (1, 2, 4, 8):
-                    if tx * ty > 256:
+                    if tx * ty > 256 or (pf == 2 and ty > 1):
                         continue
                     for m in (1, 2, 4, 8):
                         pb = ty * m
@@ -73,7 +73,7 @@ def main():
                         res.append((e0.elapsed_time(e1) / 3, pf, tx, ty, pb))
         res.sort()
         for r in res[:12]:
-            print(json.dumps({"ms": r[0], "prefetch": r[1], "tile": r[2:]}))
+            print(json.dumps({"ms": r[0], "mode": r[1], "tile": r[2:]}))
         return
     times = []
     for _ in range(args.launches):

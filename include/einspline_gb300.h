@@ -157,14 +157,18 @@ int einspline_gb300_eval_3d_sorted_noalloc(einspline_gb300_table *t, const einsp
  * lanes per block, pb points per block.  0,0,0 restores the default. */
 int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb);
 int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb);
-/* 1: before its loads, each block bulk-prefetches the stencil rows of all
- * its points into L2 (more DRAM requests in flight without registers);
- * 0: off; -1: use the autotuned choice (default off). */
-int einspline_gb300_set_prefetch(einspline_gb300_table *t, int prefetch);
-int einspline_gb300_get_prefetch(einspline_gb300_table *t);
-/* Time every candidate tile, with and without the L2 prefetch, on this
- * table for npts random points and keep the fastest (for vgh when vgh != 0);
- * the choice is cached per table. */
+/* How the kernel brings stencil rows in:
+ *   0: direct 16/8-byte loads into registers;
+ *   1: each block first bulk-prefetches the rows of all its points into L2
+ *      (more DRAM requests in flight without holding registers);
+ *   2: a three-stage pipeline of asynchronous copies into shared memory
+ *      (FP32 and 16-bit tables; one point lane per block);
+ *  -1: the autotuned choice (default 0).  Results are identical in all modes. */
+int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode);
+int einspline_gb300_get_load_mode(einspline_gb300_table *t);
+/* Time every candidate tile in every load mode on this table for npts
+ * random points and keep the fastest (for vgh when vgh != 0); the choice is
+ * cached per table. */
 int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh);
 
 /* --------------------------------------------------------------- serving */

@@ -138,13 +138,14 @@ def test_shapes_sorting_and_host_entry_are_bit_identical(orc, kind):
         got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
         for a, b in zip(got, base):
             assert np.array_equal(a, b), (tx, ty, pb)
-    G.set_prefetch(1)
-    for tx, ty, pb in [(32, 2, 8), (256, 1, 4)]:
-        G.set_tile(tx, ty, pb)
-        got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
-        for a, b in zip(got, base):
-            assert np.array_equal(a, b), ("prefetch", tx, ty, pb)
-    G.set_prefetch(-1)
+    for mode, shapes in ((1, [(32, 2, 8), (256, 1, 4)]), (2, [(32, 1, 1), (64, 1, 5), (256, 1, 16)])):
+        G.set_load_mode(mode)
+        for tx, ty, pb in shapes:
+            G.set_tile(tx, ty, pb)
+            got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
+            for a, b in zip(got, base):
+                assert np.array_equal(a, b), ("mode", mode, tx, ty, pb)
+    G.set_load_mode(-1)
     G.set_tile(0, 0, 0)
     srt = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0, sort=True)]
     for a, b in zip(srt, base):
