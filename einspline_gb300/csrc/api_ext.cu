@@ -214,7 +214,7 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode) {
   clear();
   if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
-  if (mode < -1 || mode > 2) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1 or 2");
+  if (mode < -1 || mode > 3) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1, 2 or 3");
   t->tile_mode = mode;
   return 0;
 }
@@ -283,7 +283,7 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
   const int v = vgh ? 1 : 0;
   const int saved_tuned = t->tuned_tx[v];
   t->tuned_tx[v] = 0;
-  const int nmodes = t->storage == ST_F64 ? 2 : 3;
+  const int nmodes = t->storage == ST_F64 ? 2 : (is16(t->storage) ? 4 : 3);
   for (int pf = 0; pf < nmodes; pf++) {
     t->tile_mode = pf;
     for (int tx = 32; tx <= 256; tx *= 2) {

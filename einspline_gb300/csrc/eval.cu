@@ -155,12 +155,8 @@ __device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &
 // o: v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz.
 // One x-plane i: rows (i, j, k) come from row(j, k, c); z first, then y,
 // then this plane's x terms are added to o.
-template <int ST, bool VGH, typename RowFn>
-__device__ __forceinline__ void reduce_plane(int i, const typename CT<ST>::A *w,
-                                             const typename CT<ST>::A (&wz)[3][4], RowFn row,
-                                             typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
-  using A = typename CT<ST>::A;
-  constexpr int VW = CT<ST>::VW;
+template <typename A, int VW, bool VGH, typename RowFn>
+__device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3][4], RowFn row, A (&o)[10][VW]) {
   A y[6][VW];
 #pragma unroll
   for (int q = 0; q < 6; q++)
@@ -214,16 +210,16 @@ __device__ __forceinline__ void reduce_plane(int i, const typename CT<ST>::A *w,
   }
 }
 
-template <int ST>
-__device__ __forceinline__ void zero_out(typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
+template <typename A, int VW>
+__device__ __forceinline__ void zero_out(A (&o)[10][VW]) {
 #pragma unroll
   for (int q = 0; q < 10; q++)
 #pragma unroll
-    for (int e = 0; e < CT<ST>::VW; e++) o[q][e] = typename CT<ST>::A(0);
+    for (int e = 0; e < VW; e++) o[q][e] = A(0);
 }
 
-template <int ST>
-__device__ __forceinline__ void z_weights(const typename CT<ST>::A *w, typename CT<ST>::A (&wz)[3][4]) {
+template <typename A>
+__device__ __forceinline__ void z_weights(const A *w, A (&wz)[3][4]) {
 #pragma unroll
   for (int d = 0; d < 3; d++)
 #pragma unroll
@@ -235,14 +231,15 @@ template <int ST, bool VGH>
 __device__ __forceinline__ void contract(const char *base, int64_t xsb, int64_t ysb, int64_t zsb,
                                          const typename CT<ST>::A *w, typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
   using A = typename CT<ST>::A;
-  zero_out<ST>(o);
+  constexpr int VW = CT<ST>::VW;
+  zero_out<A, VW>(o);
   A wz[3][4];
-  z_weights<ST>(w, wz);
+  z_weights<A>(w, wz);
 #pragma unroll 1
   for (int i = 0; i < 4; i++) {
     const char *plane = base + i * xsb;
-    reduce_plane<ST, VGH>(i, w, wz, [&](int j, int k, A(&c)[CT<ST>::VW]) { load_row<ST>(plane + j * ysb + k * zsb, c); },
-                          o);
+    reduce_plane<A, VW, VGH>(i, w, wz, [&](int j, int k, A(&c)[VW]) { load_row<ST>(plane + j * ysb + k * zsb, c); },
+                             o);
   }
 }
 
@@ -264,14 +261,15 @@ __device__ __forceinline__ int h9to6(int m) {
   return (m == 0) ? 0 : (m == 1 || m == 3) ? 1 : (m == 2 || m == 6) ? 2 : (m == 4) ? 3 : (m == 5 || m == 7) ? 4 : 5;
 }
 
-template <int ST, bool VGH>
-__device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col0,
-                                         typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
-  using A = typename CT<ST>::A;
-  constexpr int VW = CT<ST>::VW;
+template <typename A, int VW, bool VGH>
+__device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col0, A (&o)[10][VW]) {
   if (a.scale) {
-    const float4 s4 = *reinterpret_cast<const float4 *>(a.scale + col0);
-    const float sc[4] = {s4.x, s4.y, s4.z, s4.w};
+    float sc[VW];
+#pragma unroll
+    for (int c = 0; c < VW / 4; c++) {
+      const float4 s4 = *reinterpret_cast<const float4 *>(a.scale + col0 + 4 * c);
+      sc[4 * c] = s4.x; sc[4 * c + 1] = s4.y; sc[4 * c + 2] = s4.z; sc[4 * c + 3] = s4.w;
+    }
 #pragma unroll
     for (int q = 0; q < (VGH ? 10 : 1); q++)
 #pragma unroll
@@ -424,7 +422,7 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
     const char *base = cbase + sidx[3 * pp] * xsb + sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
     A o[10][VW];
     contract<ST, VGH>(base, xsb, ysb, zsb, sw + pp * 36, o);
-    epilogue<ST, VGH>(a, ssrc[pp], col0, o);
+    epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
   }
 }
 
@@ -465,17 +463,19 @@ constexpr int kPipeStages = 3;
 __host__ __device__ __forceinline__ size_t pipe_bytes(int nthr, int rb) { return (size_t)kPipeStages * 16 * nthr * rb; }
 
 // Pipelined variant: a stage is one x-plane (16 stencil rows) of one point.
-// Each thread copies its own VW columns of the rows of stage s+2 into shared
+// Each thread copies its own columns of the rows of stage s+2 into shared
 // memory with asynchronous copies while it reduces stage s, so the bytes in
 // flight are held in shared memory, not registers.  A thread only reads back
 // what it copied itself: the copy-group waits order it, no block barrier is
-// needed.  Same arithmetic, same order as k_eval.
-template <int ST, bool VGH>
+// needed.  WIDE (16-bit tables): 8 columns and one 16-byte copy per thread
+// and row instead of 4 columns and 8 bytes.  Same arithmetic, same order as
+// k_eval.
+template <int ST, bool VGH, bool WIDE>
 __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   using A = typename CT<ST>::A;
   using Raw = typename CT<ST>::Raw;
-  constexpr int VW = CT<ST>::VW;
-  constexpr int RB = (int)sizeof(Raw);
+  constexpr int VW = WIDE ? 2 * CT<ST>::VW : CT<ST>::VW;
+  constexpr int RB = WIDE ? 2 * (int)sizeof(Raw) : (int)sizeof(Raw);
   extern __shared__ __align__(16) unsigned char smem[];
   const int tile = blockIdx.x % a.ntiles;
   const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
@@ -508,23 +508,34 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
     cp_async_commit();
   }
   A o[10][VW];
-  zero_out<ST>(o);
+  zero_out<A, VW>(o);
+  A wz[3][4];
   for (int st = 0; st < S; st++) {
     if (st + kPipeStages - 1 < S) issue(st + kPipeStages - 1);
     cp_async_commit();
     cp_async_wait<kPipeStages - 1>();
     const int pp = st >> 2, i = st & 3;
     const A *w = sw + pp * 36;
-    A wz[3][4];
-    z_weights<ST>(w, wz);
+    if (i == 0) z_weights<A>(w, wz);
     const unsigned char *slot = pipe + (size_t)(st % kPipeStages) * slot_step + (size_t)threadIdx.x * RB;
-    reduce_plane<ST, VGH>(
+    reduce_plane<A, VW, VGH>(
         i, w, wz,
-        [&](int j, int k, A(&c)[VW]) { CT<ST>::decode(*reinterpret_cast<const Raw *>(slot + (j * 4 + k) * row_step), c); },
+        [&](int j, int k, A(&c)[VW]) {
+          const Raw *rp = reinterpret_cast<const Raw *>(slot + (j * 4 + k) * row_step);
+          if (WIDE) {
+            A lo[CT<ST>::VW], hi[CT<ST>::VW];
+            CT<ST>::decode(rp[0], lo);
+            CT<ST>::decode(rp[1], hi);
+#pragma unroll
+            for (int e = 0; e < CT<ST>::VW; e++) { c[e] = lo[e]; c[CT<ST>::VW + e] = hi[e]; }
+          } else {
+            CT<ST>::decode(rp[0], *reinterpret_cast<A(*)[CT<ST>::VW]>(&c[0]));
+          }
+        },
         o);
     if (i == 3) {
-      epilogue<ST, VGH>(a, ssrc[pp], col0, o);
-      zero_out<ST>(o);
+      epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
+      zero_out<A, VW>(o);
     }
   }
 }
@@ -544,14 +555,19 @@ void fill_eval_geometry(const Table *t, EvalArgs &a) {
   a.is_complex = t->ncomp == 2;
 }
 
+// Load modes: 0 direct, 1 L2 prefetch + direct, 2 shared-memory pipeline,
+// 3 shared-memory pipeline with 8 columns per thread (16-bit tables).
 template <int ST, bool VGH>
 static const void *kernel_for(int mode) {
-  return mode == 2 ? (const void *)k_eval_pipe<ST, VGH> : (const void *)k_eval<ST, VGH>;
+  if (mode == 2) return (const void *)k_eval_pipe<ST, VGH, false>;
+  if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
+  return (const void *)k_eval<ST, VGH>;
 }
 
 template <int ST, bool VGH>
 static cudaError_t launch_k(const EvalArgs &a, unsigned grid, dim3 block, size_t smem, cudaStream_t s) {
-  if (a.mode == 2) k_eval_pipe<ST, VGH><<<grid, block, smem, s>>>(a);
+  if (a.mode == 2) k_eval_pipe<ST, VGH, false><<<grid, block, smem, s>>>(a);
+  else if (a.mode == 3) k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)><<<grid, block, smem, s>>>(a);
   else k_eval<ST, VGH><<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -565,13 +581,14 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
     return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
   a.pb = pb;
   a.mode = pick_mode(t, vgh);
-  if (a.mode == 2 && t->storage == ST_F64) a.mode = 0;  // FP64 is FMA-bound: no pipeline variant
-  const int VW = elems_per_thread(t);
+  if (a.mode >= 2 && t->storage == ST_F64) a.mode = 0;  // FP64 is FMA-bound: no pipeline variant
+  if (a.mode == 3 && !is16(t->storage)) a.mode = 2;     // the wide variant is for 16-bit tables
+  const int VW = elems_per_thread(t) * (a.mode == 3 ? 2 : 1);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   *smem = smem_total(pb, acc_bytes(t));
-  if (a.mode == 2) {
+  if (a.mode >= 2) {
     ty = 1;
-    const int rb = t->storage == ST_F32 ? 16 : 8;
+    const int rb = (t->storage == ST_F32 || a.mode == 3) ? 16 : 8;
     *smem = align_up(*smem, 16) + pipe_bytes(tx, rb);
   }
   *block = dim3(tx, ty);

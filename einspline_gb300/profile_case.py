@@ -54,11 +54,11 @@ def main():
     torch.cuda.synchronize()
     if args.sweep:
         res = []
-        for pf in (0, 1, 2):
+        for pf in (0, 1, 2, 3):
             T.set_load_mode(pf)
             for tx in (32, 64, 128, 256):
                 for ty in (1, 2, 4, 8):
-                    if tx * ty > 256 or (pf == 2 and ty > 1):
+                    if tx * ty > 256 or (pf >= 2 and ty > 1):
                         continue
                     for m in (1, 2, 4, 8):
                         pb = ty * m

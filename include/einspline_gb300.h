@@ -163,6 +163,8 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  *      (more DRAM requests in flight without holding registers);
  *   2: a three-stage pipeline of asynchronous copies into shared memory
  *      (FP32 and 16-bit tables; one point lane per block);
+ *   3: as 2 with 8 columns and one 16-byte copy per thread and row (16-bit
+ *      tables; others use 2);
  *  -1: the autotuned choice (default 0).  Results are identical in all modes. */
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode);
 int einspline_gb300_get_load_mode(einspline_gb300_table *t);

@@ -138,7 +138,8 @@ def test_shapes_sorting_and_host_entry_are_bit_identical(orc, kind):
         got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
         for a, b in zip(got, base):
             assert np.array_equal(a, b), (tx, ty, pb)
-    for mode, shapes in ((1, [(32, 2, 8), (256, 1, 4)]), (2, [(32, 1, 1), (64, 1, 5), (256, 1, 16)])):
+    for mode, shapes in ((1, [(32, 2, 8), (256, 1, 4)]), (2, [(32, 1, 1), (64, 1, 5), (256, 1, 16)]),
+                         (3, [(32, 1, 3), (128, 1, 8)])):
         G.set_load_mode(mode)
         for tx, ty, pb in shapes:
             G.set_tile(tx, ty, pb)
