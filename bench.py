@@ -260,6 +260,7 @@ def run_gpu(args):
 
     for t in tabs.values():
         tune(t)
+    tiles = {k: {"tile": list(t.get_tile()), "load_mode": t.get_load_mode()} for k, t in tabs.items()}
 
     def timed(t, sort=False):
         for k in range(args.warmup):
@@ -359,6 +360,7 @@ def run_gpu(args):
     err = None
     if rank == 0 and args.error_points > 0:
         err = precision_report(tabs, args.error_points)
+    other = other_configs(args) if (rank == 0 and args.configs) else None
 
     if rank != 0:
         return
@@ -369,6 +371,7 @@ def run_gpu(args):
         "config": workload_config(),
         "fp32_table": {"value": rate32, "ms_per_step": ms32 / args.steps, "launches": l32},
         "fp16_vs_fp32": rate16 / rate32,
+        "tiles": tiles,
         "i16_table": {"value": evi / (msi / 1e3), "ms_per_step": msi / args.steps},
         "cell_sorted": {"f16_value": ev16s / (ms16s / 1e3), "f32_value": ev32s / (ms32s / 1e3),
                         "launches_per_step": l16s / max(1, args.steps),
@@ -389,6 +392,7 @@ def run_gpu(args):
         "gpu_launches": l16,
         "clocks": clk.summary(),
         "error_vs_fp64": err,
+        "other_configs": other,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -429,6 +433,68 @@ def precision_report(tabs, npts):
     return rep
 
 
+def other_configs(args):
+    """Throughput of the other workloads (parity-test configurations, not
+    the headline): C2 FP64 48^3 x 512 plane waves, 128 x 256 points; C3
+    complex 64^3 x 256, 256 x 128 points, random vs cell-sorted; C5 FP32/F16
+    128^3 x 2048, chunks of 256 walkers x 256 points."""
+    import torch
+    from einspline_gb300 import api, synth
+    out = {}
+
+    def rate(t, pos, reps=10, sort=False, out_bufs=None):
+        t.eval(pos, sort=sort, out=out_bufs)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            t.eval(pos, sort=sort, out=out_bufs)
+        e1.record()
+        torch.cuda.synchronize()
+        return pos.shape[0] * t.N * reps / (e0.elapsed_time(e1) / 1e3)
+
+    def dev_table(kind, M, N, seed, storage=api.STORE_NATIVE):
+        t = api.MultiUBspline3D(kind, [(0.0, 1.0, M)] * 3, [(api.PERIODIC, api.PERIODIC)] * 3, N, storage=storage)
+        per = M ** 3 * (2 if kind in "cz" else 1)
+        dt = torch.float32 if kind in "sc" else torch.float64
+        chunk = max(1, min(N, (512 << 20) // (per * 8)))
+        buf = torch.empty((chunk,) + (M, M, M) + ((2,) if kind in "cz" else ()), dtype=dt, device="cuda")
+        for f in range(0, N, chunk):
+            n = min(chunk, N - f)
+            api.fill_uniform(buf[:n], seed, -1.0, 1.0, offset=f * per)
+            t.set_device(f, buf[:n])
+        t.flush()
+        del buf
+        return t
+
+    t = dev_table("d", 48, 512, 202)
+    t.autotune(128 * 256)
+    p = torch.from_numpy(synth.points_uniform(203, 128 * 256)).cuda()
+    r = rate(t, p)
+    out["C2_d_48cube_512"] = {"evals_per_s": r, "GBps_alg": r * 592 / 1e9, "tile": list(t.get_tile())}
+    del t
+    t = dev_table("c", 64, 256, 303)
+    t.autotune(256 * 128)
+    p = torch.from_numpy(synth.points_uniform(304, 256 * 128)).cuda()
+    out["C3_c_64cube_256"] = {"random_evals_per_s": rate(t, p), "sorted_evals_per_s": rate(t, p, sort=True),
+                              "GBps_alg_random": rate(t, p) * 592 / 1e9}
+    del t
+    for name, st, bpe in (("f32", api.STORE_F32, 296), ("f16", api.STORE_F16, 168)):
+        t = dev_table("s", 128, 2048, 505, storage=st)
+        t.autotune(16384)
+        P = 256 * 256
+        p = torch.from_numpy(synth.points_uniform(506, P)).cuda()
+        bufs = (torch.empty((P, 2048), device="cuda"), torch.empty((P, 2048, 3), device="cuda"),
+                torch.empty((P, 2048, 6), device="cuda"))
+        r = rate(t, p, reps=3, out_bufs=bufs)
+        out[f"C5_s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9,
+                                            "note": "256 walkers x 256 points per launch (the 4096-walker step "
+                                                    "is 16 such launches; outputs of all 4096 would be 84 GB)"}
+        del t, bufs
+        torch.cuda.empty_cache()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -441,6 +507,7 @@ def main():
     ap.add_argument("--load", type=float, nargs="*", default=[0.5, 0.9])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--error-points", type=int, default=256)
+    ap.add_argument("--configs", type=int, default=0, help="also time the other BASELINE configurations")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
