@@ -116,12 +116,18 @@ def _signatures():
         sig[f"set_multi_UBspline_3d_{k}"] = ([H, i32, vp], None)
         sig[f"eval_multi_UBspline_3d_{k}"] = ([H, dbl, dbl, dbl, vp], None)
         sig[f"eval_multi_UBspline_3d_{k}_vgh"] = ([H, dbl, dbl, dbl, vp, vp, vp], None)
+        sig[f"eval_multi_UBspline_3d_{k}_vg"] = ([H, dbl, dbl, dbl, vp, vp], None)
+        sig[f"eval_multi_UBspline_3d_{k}_vgl"] = ([H, dbl, dbl, dbl, vp, vp, vp], None)
+        sig[f"eval_multi_multi_UBspline_3d_{k}_vgl_cuda"] = ([D, vp, vp, vp, vp, i32, i32], None)
         sig[f"create_multi_UBspline_3d_{k}_cuda"] = ([H], D)
         sig[f"destroy_multi_UBspline_3d_{k}_cuda"] = ([D], None)
         sig[f"eval_multi_multi_UBspline_3d_{k}_cuda"] = ([D, vp, vp, i32], None)
         sig[f"eval_multi_multi_UBspline_3d_{k}_vgh_cuda"] = ([D, vp, vp, vp, vp, i32], None)
     sig["create_multi_UBspline_3d_s_cuda_conv"] = ([C.POINTER(HOST_STRUCTS["d"])], C.POINTER(CUDA_STRUCTS["s"]))
     sig["create_multi_UBspline_3d_c_cuda_conv"] = ([C.POINTER(HOST_STRUCTS["z"])], C.POINTER(CUDA_STRUCTS["c"]))
+    sig["eval_multi_multi_UBspline_3d_s_sign_cuda"] = ([C.POINTER(CUDA_STRUCTS["s"]), vp, vp, vp, i32], None)
+    sig["eval_multi_multi_UBspline_3d_s_vgl_sign_cuda"] = ([C.POINTER(CUDA_STRUCTS["s"]), vp, vp, vp, vp, vp, i32,
+                                                            i32], None)
     sig["destroy_Bspline"] = ([vp], None)
     sig["destroy_multi_UBspline"] = ([vp], None)
     sig["einspline_gb300_create_3d_s"] = ([Ugrid, Ugrid, Ugrid, BCtype_s, BCtype_s, BCtype_s, i32, i32],

@@ -164,6 +164,28 @@ class MultiUBspline3D:
         check()
         return v, None, None
 
+    def eval_point_vg(self, x: float, y: float, z: float):
+        """eval_multi_UBspline_3d_*_vg: (vals, grads) at one point."""
+        dt = out_dtype(self.kind)
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((self.N,) + ext, dt)
+        g = np.zeros((self.N, 3) + ext, dt)
+        getattr(_lib(), f"eval_multi_UBspline_3d_{self.kind}_vg")(self.ptr, x, y, z, v.ctypes.data, g.ctypes.data)
+        check()
+        return v, g
+
+    def eval_point_vgl(self, x: float, y: float, z: float):
+        """eval_multi_UBspline_3d_*_vgl: (vals, grads, lapl) at one point."""
+        dt = out_dtype(self.kind)
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((self.N,) + ext, dt)
+        g = np.zeros((self.N, 3) + ext, dt)
+        lap = np.zeros((self.N,) + ext, dt)
+        getattr(_lib(), f"eval_multi_UBspline_3d_{self.kind}_vgl")(self.ptr, x, y, z, v.ctypes.data, g.ctypes.data,
+                                                                   lap.ctypes.data)
+        check()
+        return v, g, lap
+
     def out_shapes(self, P, layout):
         ext = (2,) if self.ncomp == 2 else ()
         if layout == 0:
@@ -283,6 +305,43 @@ class CudaSpline:
                 self.ptr, C.c_void_p(pos.data_ptr()), C.c_void_p(vp.data_ptr()), P)
         check()
         return v, g, h
+
+    def eval_multi_sign(self, pos, sign):
+        """eval_multi_multi_UBspline_3d_s_sign_cuda: values times sign[i]."""
+        torch = _torch()
+        P = int(pos.shape[0])
+        v = torch.zeros((P, self.N), dtype=torch.float32, device=pos.device)
+        vp = torch.tensor([v.data_ptr() + i * self.N * 4 for i in range(P)], dtype=torch.int64, device=pos.device)
+        _lib().eval_multi_multi_UBspline_3d_s_sign_cuda(self.ptr, C.c_void_p(pos.data_ptr()),
+                                                        C.c_void_p(sign.data_ptr()), C.c_void_p(vp.data_ptr()), P)
+        check()
+        return v
+
+    def eval_multi_vgl(self, pos, linv, row_stride=None, sign=None):
+        """eval_multi_multi_UBspline_3d_*_vgl_cuda (or _s_vgl_sign_cuda): returns
+        (vals [P][N*ncomp], grad_lapl [P][4][row_stride*ncomp])."""
+        torch = _torch()
+        P = int(pos.shape[0])
+        dt = torch.float32 if self.kind in "sc" else torch.float64
+        nr = self.N * self.ncomp
+        rs = row_stride if row_stride is not None else self.N
+        v = torch.zeros((P, nr), dtype=dt, device=pos.device)
+        gl = torch.full((P, 4, rs * self.ncomp), -7.0, dtype=dt, device=pos.device)
+        es = v.element_size()
+        vp = torch.tensor([v.data_ptr() + i * nr * es for i in range(P)], dtype=torch.int64, device=pos.device)
+        gp = torch.tensor([gl.data_ptr() + i * 4 * rs * self.ncomp * es for i in range(P)], dtype=torch.int64,
+                          device=pos.device)
+        lib = _lib()
+        if sign is not None:
+            lib.eval_multi_multi_UBspline_3d_s_vgl_sign_cuda(self.ptr, C.c_void_p(pos.data_ptr()),
+                                                             C.c_void_p(sign.data_ptr()), C.c_void_p(linv.data_ptr()),
+                                                             C.c_void_p(vp.data_ptr()), C.c_void_p(gp.data_ptr()), P, rs)
+        else:
+            getattr(lib, f"eval_multi_multi_UBspline_3d_{self.kind}_vgl_cuda")(
+                self.ptr, C.c_void_p(pos.data_ptr()), C.c_void_p(linv.data_ptr()), C.c_void_p(vp.data_ptr()),
+                C.c_void_p(gp.data_ptr()), P, rs)
+        check()
+        return v, gl
 
     def destroy(self):
         if getattr(self, "ptr", None):

@@ -167,7 +167,14 @@ struct EvalArgs {
   int ntiles;                 // column tiles per point group
   int pb;                     // points per block
   int mode;                   // load mode: 0 direct loads, 1 L2 bulk prefetch first,
-                              // 2 shared-memory pipeline of async copies
+                              // 2/3 shared-memory pipeline of async copies
+  int out;                    // 0 vgh; 1 vgl with lattice transform (GPU entries):
+                              // 4 rows G.grad and Tr(G^T G H) at lrow apart in gl_pp;
+                              // 2 vgl (CPU entries): grads and lapl = trace(H) in hess;
+                              // 3 vg: value and gradient only
+  const void *sign;           // optional per-point factor (output type) on every output
+  const void *linv;           // out 1: 3x3 row-major G (output type)
+  int64_t lrow;               // out 1: row stride of the gradient/laplacian rows (reals)
 };
 
 int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb);

@@ -285,6 +285,13 @@ __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col
 #pragma unroll
       for (int e = 0; e < VW; e++) o[q][e] *= f[q];
   }
+  if (a.sign) {
+    const A sg = reinterpret_cast<const A *>(a.sign)[src];
+#pragma unroll
+    for (int q = 0; q < (VGH ? 10 : 1); q++)
+#pragma unroll
+      for (int e = 0; e < VW; e++) o[q][e] *= sg;
+  }
   A *vp = a.vals_pp ? (A *)a.vals_pp[src] : (A *)a.vals + src * a.vstride;
   const bool full = col0 + VW <= a.ncol;
   {
@@ -298,6 +305,40 @@ __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col
         if (col0 + e < a.ncol) vp[col0 + e] = v[e];
   }
   if (!VGH) return;
+  if (a.out == 1) {
+    // Lattice transform (src/multi_bspline_cuda_s_impl.h:706-733): rows
+    // G.grad (3) and Tr(G^T G H), each lrow reals apart.
+    const A *L = reinterpret_cast<const A *>(a.linv);
+    A G[9];
+#pragma unroll
+    for (int m = 0; m < 9; m++) G[m] = L[m];
+    A GG[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) GG[r][c] = G[r] * G[c] + G[3 + r] * G[3 + c] + G[6 + r] * G[6 + c];
+    A *gl = (A *)a.grads_pp[src];
+    A row[4][VW];
+#pragma unroll
+    for (int e = 0; e < VW; e++) {
+      const A gx = o[1][e], gy = o[2][e], gz = o[3][e];
+      const A hxx = o[4][e], hxy = o[5][e], hxz = o[6][e], hyy = o[7][e], hyz = o[8][e], hzz = o[9][e];
+#pragma unroll
+      for (int r = 0; r < 3; r++) row[r][e] = G[3 * r] * gx + G[3 * r + 1] * gy + G[3 * r + 2] * gz;
+      row[3][e] = GG[0][0] * hxx + GG[1][0] * hxy + GG[2][0] * hxz + GG[0][1] * hxy + GG[1][1] * hyy +
+                  GG[2][1] * hyz + GG[0][2] * hxz + GG[1][2] * hyz + GG[2][2] * hzz;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      A *rp = gl + r * a.lrow + col0;
+      if (full && al16(rp)) st_vec<VW>(rp, row[r]);
+      else
+#pragma unroll
+        for (int e = 0; e < VW; e++)
+          if (col0 + e < a.ncol) rp[e] = row[r][e];
+    }
+    return;
+  }
   A *gp = a.grads_pp ? (A *)a.grads_pp[src] : (A *)a.grads + src * a.gstride;
   A *hp = a.hess_pp ? (A *)a.hess_pp[src] : (A *)a.hess + src * a.hstride;
   const bool cpx_cpu = a.is_complex && a.layout == 1;
@@ -321,6 +362,20 @@ __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col
             const int idx = cpx_cpu ? 6 * (e >> 1) + 2 * c + (e & 1) : 3 * e + c;
             gb[idx] = g[idx];
           }
+  }
+  if (a.out == 3) return;
+  if (a.out == 2) {
+    // CPU vgl (src/multi_bspline_eval_std_s_impl.h:724-731): lapl = (xx + yy) + zz.
+    A l[VW];
+#pragma unroll
+    for (int e = 0; e < VW; e++) l[e] = (o[4][e] + o[7][e]) + o[9][e];
+    A *lb = hp + col0;
+    if (full && al16(lb)) st_vec<VW>(lb, l);
+    else
+#pragma unroll
+      for (int e = 0; e < VW; e++)
+        if (col0 + e < a.ncol) lb[e] = l[e];
+    return;
   }
   if (a.layout == 0) {
     A h[6 * VW];
@@ -677,9 +732,10 @@ Table *host_table(S *s, const char *fn) {
   return s->gb300;
 }
 
-// Single point, host outputs in the CPU layout.
+// Single point, host outputs in the CPU layout.  out: 0 vgh, 2 vgl, 3 vg.
 template <typename S, typename V>
-void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, bool vgh, const char *fn) {
+void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, bool vgh, const char *fn,
+                int out = 0) {
   clear();
   Table *t = host_table(s, fn);
   if (!t) return;
@@ -702,6 +758,7 @@ void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, 
   a.inl[0] = x; a.inl[1] = y; a.inl[2] = z;
   a.rule = 0;
   a.layout = 1;
+  a.out = out;
   a.npts = 1;
   a.vals = t->pt_dev;
   a.grads = (char *)t->pt_dev + n * rb;
@@ -718,14 +775,17 @@ void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, 
   memcpy(vals, t->pt_host, n * rb);
   if (vgh) {
     memcpy(grads, (char *)t->pt_host + n * rb, 3 * n * rb);
-    memcpy(hess, (char *)t->pt_host + 4 * n * rb, 9 * n * rb);
+    if (out == 0) memcpy(hess, (char *)t->pt_host + 4 * n * rb, 9 * n * rb);
+    if (out == 2) memcpy(hess, (char *)t->pt_host + 4 * n * rb, n * rb);
   }
 }
 
 // Batched, reference GPU-entry semantics and layout, pointer-array outputs.
+// out 1 (vgl): grads_d holds the grad_lapl pointers, linv/lrow the transform.
 template <typename CS>
 void eval_cuda(CS *c, const void *pos_d, bool pos_f64, void *const *vals_d, void *const *grads_d,
-               void *const *hess_d, int num, bool vgh, const char *fn) {
+               void *const *hess_d, int num, bool vgh, const char *fn, int out = 0, const void *sign = nullptr,
+               const void *linv = nullptr, int64_t lrow = 0) {
   clear();
   if (!c || !table_ok(c->gb300)) { fail(EINSPLINE_GB300_EINVAL, "%s: not a handle made by this library", fn); return; }
   if (num <= 0) return;
@@ -739,6 +799,11 @@ void eval_cuda(CS *c, const void *pos_d, bool pos_f64, void *const *vals_d, void
   a.layout = 0;
   a.npts = num;
   a.vals_pp = vals_d; a.grads_pp = grads_d; a.hess_pp = hess_d;
+  a.out = out;
+  a.sign = sign;
+  a.linv = linv;
+  a.lrow = lrow;
+  if (out == 1 && (!linv || !grads_d)) { fail(EINSPLINE_GB300_EINVAL, "%s: Linv and grad_lapl are required", fn); return; }
   int tx, ty, pb;
   pick_tile(t, vgh, num, tx, ty, pb);
   if (launch_eval(t, a, vgh, cudaStreamLegacy, tx, ty, pb)) return;
@@ -781,6 +846,79 @@ void eval_multi_UBspline_3d_z_vgh(multi_UBspline_3d_z *s, double x, double y, do
                                   complex_double *grads, complex_double *hess) {
   eval_point<multi_UBspline_3d_z, complex_double>(s, x, y, z, vals, grads, hess, true,
                                                   "eval_multi_UBspline_3d_z_vgh");
+}
+
+void eval_multi_UBspline_3d_s_vg(multi_UBspline_3d_s *s, double x, double y, double z, float *vals, float *grads) {
+  eval_point<multi_UBspline_3d_s, float>(s, x, y, z, vals, grads, nullptr, true, "eval_multi_UBspline_3d_s_vg", 3);
+}
+void eval_multi_UBspline_3d_s_vgl(multi_UBspline_3d_s *s, double x, double y, double z, float *vals, float *grads,
+                                  float *lapl) {
+  eval_point<multi_UBspline_3d_s, float>(s, x, y, z, vals, grads, lapl, true, "eval_multi_UBspline_3d_s_vgl", 2);
+}
+void eval_multi_UBspline_3d_d_vg(multi_UBspline_3d_d *s, double x, double y, double z, double *vals, double *grads) {
+  eval_point<multi_UBspline_3d_d, double>(s, x, y, z, vals, grads, nullptr, true, "eval_multi_UBspline_3d_d_vg", 3);
+}
+void eval_multi_UBspline_3d_d_vgl(multi_UBspline_3d_d *s, double x, double y, double z, double *vals, double *grads,
+                                  double *lapl) {
+  eval_point<multi_UBspline_3d_d, double>(s, x, y, z, vals, grads, lapl, true, "eval_multi_UBspline_3d_d_vgl", 2);
+}
+void eval_multi_UBspline_3d_c_vg(multi_UBspline_3d_c *s, double x, double y, double z, complex_float *vals,
+                                 complex_float *grads) {
+  eval_point<multi_UBspline_3d_c, complex_float>(s, x, y, z, vals, grads, nullptr, true,
+                                                 "eval_multi_UBspline_3d_c_vg", 3);
+}
+void eval_multi_UBspline_3d_c_vgl(multi_UBspline_3d_c *s, double x, double y, double z, complex_float *vals,
+                                  complex_float *grads, complex_float *lapl) {
+  eval_point<multi_UBspline_3d_c, complex_float>(s, x, y, z, vals, grads, lapl, true,
+                                                 "eval_multi_UBspline_3d_c_vgl", 2);
+}
+void eval_multi_UBspline_3d_z_vg(multi_UBspline_3d_z *s, double x, double y, double z, complex_double *vals,
+                                 complex_double *grads) {
+  eval_point<multi_UBspline_3d_z, complex_double>(s, x, y, z, vals, grads, nullptr, true,
+                                                  "eval_multi_UBspline_3d_z_vg", 3);
+}
+void eval_multi_UBspline_3d_z_vgl(multi_UBspline_3d_z *s, double x, double y, double z, complex_double *vals,
+                                  complex_double *grads, complex_double *lapl) {
+  eval_point<multi_UBspline_3d_z, complex_double>(s, x, y, z, vals, grads, lapl, true,
+                                                  "eval_multi_UBspline_3d_z_vgl", 2);
+}
+
+void eval_multi_multi_UBspline_3d_s_sign_cuda(multi_UBspline_3d_s_cuda *c, float *pos_d, float *sign_d,
+                                              float *vals_d[], int num) {
+  if (!sign_d) { clear(); fail(EINSPLINE_GB300_EINVAL, "eval_multi_multi_UBspline_3d_s_sign_cuda: sign_d is NULL"); return; }
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, nullptr, nullptr, num, false,
+            "eval_multi_multi_UBspline_3d_s_sign_cuda", 0, sign_d);
+}
+void eval_multi_multi_UBspline_3d_s_vgl_cuda(multi_UBspline_3d_s_cuda *c, float *pos_d, float *Linv_d,
+                                             float *vals_d[], float *grad_lapl_d[], int num, int row_stride) {
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, (void *const *)grad_lapl_d, nullptr, num, true,
+            "eval_multi_multi_UBspline_3d_s_vgl_cuda", 1, nullptr, Linv_d, row_stride);
+}
+void eval_multi_multi_UBspline_3d_s_vgl_sign_cuda(multi_UBspline_3d_s_cuda *c, float *pos_d, float *sign_d,
+                                                  float *Linv_d, float *vals_d[], float *grad_lapl_d[], int num,
+                                                  int row_stride) {
+  if (!sign_d) { clear(); fail(EINSPLINE_GB300_EINVAL, "eval_multi_multi_UBspline_3d_s_vgl_sign_cuda: sign_d is NULL"); return; }
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, (void *const *)grad_lapl_d, nullptr, num, true,
+            "eval_multi_multi_UBspline_3d_s_vgl_sign_cuda", 1, sign_d, Linv_d, row_stride);
+}
+void eval_multi_multi_UBspline_3d_d_vgl_cuda(multi_UBspline_3d_d_cuda *c, double *pos_d, double *Linv_d,
+                                             double *vals_d[], double *grad_lapl_d[], int num, int row_stride) {
+  eval_cuda(c, pos_d, true, (void *const *)vals_d, (void *const *)grad_lapl_d, nullptr, num, true,
+            "eval_multi_multi_UBspline_3d_d_vgl_cuda", 1, nullptr, Linv_d, row_stride);
+}
+// Complex rows are row_stride complex values apart: 2 * row_stride reals
+// (src/multi_bspline_cuda_c_impl.h:612-622).
+void eval_multi_multi_UBspline_3d_c_vgl_cuda(multi_UBspline_3d_c_cuda *c, float *pos_d, float *Linv_d,
+                                             complex_float *vals_d[], complex_float *grad_lapl_d[], int num,
+                                             int row_stride) {
+  eval_cuda(c, pos_d, false, (void *const *)vals_d, (void *const *)grad_lapl_d, nullptr, num, true,
+            "eval_multi_multi_UBspline_3d_c_vgl_cuda", 1, nullptr, Linv_d, 2 * (int64_t)row_stride);
+}
+void eval_multi_multi_UBspline_3d_z_vgl_cuda(multi_UBspline_3d_z_cuda *c, double *pos_d, double *Linv_d,
+                                             complex_double *vals_d[], complex_double *grad_lapl_d[], int num,
+                                             int row_stride) {
+  eval_cuda(c, pos_d, true, (void *const *)vals_d, (void *const *)grad_lapl_d, nullptr, num, true,
+            "eval_multi_multi_UBspline_3d_z_vgl_cuda", 1, nullptr, Linv_d, 2 * (int64_t)row_stride);
 }
 
 void eval_multi_multi_UBspline_3d_s_cuda(multi_UBspline_3d_s_cuda *c, float *pos_d, float *vals_d[], int num) {

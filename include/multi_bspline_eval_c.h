@@ -2,7 +2,7 @@
  * multi_bspline_eval_c.h -- single-point evaluation of a uniform 3D
  * multi-spline of type c (complex_float), host output buffers.
  *
- * Replaces the 3D value and vgh entries of src/multi_bspline_eval_c.h:92-115.
+ * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_c.h:92-115.
  * Output layout is the reference CPU layout: vals[N], grads[N][3],
  * hess[N][3][3] (full symmetric matrix, row-major).  The point may be given
  * anywhere; the reference reads outside its table when a point leaves
@@ -21,6 +21,14 @@ extern "C" {
 
 void eval_multi_UBspline_3d_c(multi_UBspline_3d_c *spline, double x, double y, double z,
                                complex_float *vals);
+
+/* src/multi_bspline_eval_c.h:97-108: value and gradient, grads[N][3]. */
+void eval_multi_UBspline_3d_c_vg(multi_UBspline_3d_c *spline, double x, double y, double z,
+                                  complex_float *vals, complex_float *grads);
+
+/* src/multi_bspline_eval_c.h:97-108: value, gradient and laplacian (d2/dx2 + d2/dy2 + d2/dz2), lapl[N]. */
+void eval_multi_UBspline_3d_c_vgl(multi_UBspline_3d_c *spline, double x, double y, double z,
+                                   complex_float *vals, complex_float *grads, complex_float *lapl);
 
 void eval_multi_UBspline_3d_c_vgh(multi_UBspline_3d_c *spline, double x, double y, double z,
                                    complex_float *vals, complex_float *grads, complex_float *hess);

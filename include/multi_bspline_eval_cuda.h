@@ -1,7 +1,7 @@
 /*
  * multi_bspline_eval_cuda.h -- batched multi-point evaluation on the GPU.
  *
- * Replaces the 3D value and vgh entries of src/multi_bspline_eval_cuda.h:62-132
+ * Replaces the 3D value, sign, vgh and vgl entries of src/multi_bspline_eval_cuda.h:62-137
  * (kernels and launchers in src/multi_bspline_cuda_{s,d,c,z}_impl.h).
  * Same arguments and meaning:
  *   pos_d   device array of num points, xyz interleaved (float for s/c,
@@ -35,6 +35,21 @@ void eval_multi_multi_UBspline_3d_s_vgh_cuda(multi_UBspline_3d_s_cuda *spline, f
                                              float *vals_d[], float *grads_d[], float *hess_d[],
                                              int num);
 
+/* src/multi_bspline_eval_cuda.h:67-68; src/multi_bspline_cuda_s_impl.h:515: values times
+ * a per-point factor sign_d[i] (device array of num floats). */
+void eval_multi_multi_UBspline_3d_s_sign_cuda(multi_UBspline_3d_s_cuda *spline, float *pos_d, float *sign_d,
+                                              float *vals_d[], int num);
+/* src/multi_bspline_eval_cuda.h:77-79; src/multi_bspline_cuda_s_impl.h:566-760: value, and
+ * four rows at grad_lapl_d[i] + r*row_stride: G.grad (r = 0,1,2) and the laplacian
+ * Tr(G^T G H) (r = 3), with G = Linv_d (device, 3x3 row-major). */
+void eval_multi_multi_UBspline_3d_s_vgl_cuda(multi_UBspline_3d_s_cuda *spline, float *pos_d, float *Linv_d,
+                                             float *vals_d[], float *grad_lapl_d[], int num, int row_stride);
+/* src/multi_bspline_eval_cuda.h:82-84; src/multi_bspline_cuda_s_impl.h:763-933: vgl times
+ * the per-point factor sign_d[i]. */
+void eval_multi_multi_UBspline_3d_s_vgl_sign_cuda(multi_UBspline_3d_s_cuda *spline, float *pos_d, float *sign_d,
+                                                  float *Linv_d, float *vals_d[], float *grad_lapl_d[], int num,
+                                                  int row_stride);
+
 /* src/multi_bspline_eval_cuda.h:89-91; src/multi_bspline_cuda_d_impl.h:229 */
 void eval_multi_multi_UBspline_3d_d_cuda(multi_UBspline_3d_d_cuda *spline, double *pos_d,
                                          double *vals_d[], int num);
@@ -42,6 +57,10 @@ void eval_multi_multi_UBspline_3d_d_cuda(multi_UBspline_3d_d_cuda *spline, doubl
 void eval_multi_multi_UBspline_3d_d_vgh_cuda(multi_UBspline_3d_d_cuda *spline, double *pos_d,
                                              double *vals_d[], double *grads_d[],
                                              double *hess_d[], int num);
+
+/* src/multi_bspline_eval_cuda.h:99-101; src/multi_bspline_cuda_d_impl.h:278-452 */
+void eval_multi_multi_UBspline_3d_d_vgl_cuda(multi_UBspline_3d_d_cuda *spline, double *pos_d, double *Linv_d,
+                                             double *vals_d[], double *grad_lapl_d[], int num, int row_stride);
 
 /* src/multi_bspline_eval_cuda.h:105-108; src/multi_bspline_cuda_c_impl.h:417 */
 void eval_multi_multi_UBspline_3d_c_cuda(multi_UBspline_3d_c_cuda *spline, float *pos_d,
@@ -51,6 +70,12 @@ void eval_multi_multi_UBspline_3d_c_vgh_cuda(multi_UBspline_3d_c_cuda *spline, f
                                              complex_float *vals_d[], complex_float *grads_d[],
                                              complex_float *hess_d[], int num);
 
+/* src/multi_bspline_eval_cuda.h:117-119; src/multi_bspline_cuda_c_impl.h:467-660: rows are
+ * row_stride complex values apart. */
+void eval_multi_multi_UBspline_3d_c_vgl_cuda(multi_UBspline_3d_c_cuda *spline, float *pos_d, float *Linv_d,
+                                             complex_float *vals_d[], complex_float *grad_lapl_d[], int num,
+                                             int row_stride);
+
 /* src/multi_bspline_eval_cuda.h:123-126; src/multi_bspline_cuda_z_impl.h:233 */
 void eval_multi_multi_UBspline_3d_z_cuda(multi_UBspline_3d_z_cuda *spline, double *pos_d,
                                          complex_double *vals_d[], int num);
@@ -58,6 +83,11 @@ void eval_multi_multi_UBspline_3d_z_cuda(multi_UBspline_3d_z_cuda *spline, doubl
 void eval_multi_multi_UBspline_3d_z_vgh_cuda(multi_UBspline_3d_z_cuda *spline, double *pos_d,
                                              complex_double *vals_d[], complex_double *grads_d[],
                                              complex_double *hess_d[], int num);
+
+/* src/multi_bspline_eval_cuda.h:135-137; src/multi_bspline_cuda_z_impl.h:284-458 */
+void eval_multi_multi_UBspline_3d_z_vgl_cuda(multi_UBspline_3d_z_cuda *spline, double *pos_d, double *Linv_d,
+                                             complex_double *vals_d[], complex_double *grad_lapl_d[], int num,
+                                             int row_stride);
 
 #ifdef __cplusplus
 }

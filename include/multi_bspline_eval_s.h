@@ -2,7 +2,7 @@
  * multi_bspline_eval_s.h -- single-point evaluation of a uniform 3D
  * multi-spline of type s (float), host output buffers.
  *
- * Replaces the 3D value and vgh entries of src/multi_bspline_eval_s.h:87-110.
+ * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_s.h:87-110.
  * Output layout is the reference CPU layout: vals[N], grads[N][3],
  * hess[N][3][3] (full symmetric matrix, row-major).  The point may be given
  * anywhere; the reference reads outside its table when a point leaves
@@ -21,6 +21,14 @@ extern "C" {
 
 void eval_multi_UBspline_3d_s(multi_UBspline_3d_s *spline, double x, double y, double z,
                                float *vals);
+
+/* src/multi_bspline_eval_s.h:92-103: value and gradient, grads[N][3]. */
+void eval_multi_UBspline_3d_s_vg(multi_UBspline_3d_s *spline, double x, double y, double z,
+                                  float *vals, float *grads);
+
+/* src/multi_bspline_eval_s.h:92-103: value, gradient and laplacian (d2/dx2 + d2/dy2 + d2/dz2), lapl[N]. */
+void eval_multi_UBspline_3d_s_vgl(multi_UBspline_3d_s *spline, double x, double y, double z,
+                                   float *vals, float *grads, float *lapl);
 
 void eval_multi_UBspline_3d_s_vgh(multi_UBspline_3d_s *spline, double x, double y, double z,
                                    float *vals, float *grads, float *hess);

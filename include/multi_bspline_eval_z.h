@@ -2,7 +2,7 @@
  * multi_bspline_eval_z.h -- single-point evaluation of a uniform 3D
  * multi-spline of type z (complex_double), host output buffers.
  *
- * Replaces the 3D value and vgh entries of src/multi_bspline_eval_z.h:87-110.
+ * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_z.h:87-110.
  * Output layout is the reference CPU layout: vals[N], grads[N][3],
  * hess[N][3][3] (full symmetric matrix, row-major).  The point may be given
  * anywhere; the reference reads outside its table when a point leaves
@@ -21,6 +21,14 @@ extern "C" {
 
 void eval_multi_UBspline_3d_z(multi_UBspline_3d_z *spline, double x, double y, double z,
                                complex_double *vals);
+
+/* src/multi_bspline_eval_z.h:92-103: value and gradient, grads[N][3]. */
+void eval_multi_UBspline_3d_z_vg(multi_UBspline_3d_z *spline, double x, double y, double z,
+                                  complex_double *vals, complex_double *grads);
+
+/* src/multi_bspline_eval_z.h:92-103: value, gradient and laplacian (d2/dx2 + d2/dy2 + d2/dz2), lapl[N]. */
+void eval_multi_UBspline_3d_z_vgl(multi_UBspline_3d_z *spline, double x, double y, double z,
+                                   complex_double *vals, complex_double *grads, complex_double *lapl);
 
 void eval_multi_UBspline_3d_z_vgh(multi_UBspline_3d_z *spline, double x, double y, double z,
                                    complex_double *vals, complex_double *grads, complex_double *hess);
