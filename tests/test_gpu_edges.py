@@ -1,0 +1,99 @@
+"""Edge cases: batches beyond the reference's 65,535-point launch limit,
+tiny and odd spline counts, non-periodic tables through the reference-shaped
+entry, strided host outputs, and argument errors reported as status codes."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from einspline_gb300 import _lib as L
+from einspline_gb300 import api, synth
+
+from helpers import TOL, assert_close, build_pair, cpu_to_gpu_layout, table_box
+
+P, D1, D2, FL, NA, AP = 0, 1, 2, 3, 4, 5
+
+
+@pytest.mark.gpu
+def test_more_points_than_reference_grid_limit(orc):
+    import torch
+    G, T, _ = build_pair(orc, "s", [(0.0, 1.0, 10)] * 3, [(P, P)] * 3, 5, seed=91)
+    c = G.to_cuda()
+    n = 70000
+    pos = synth.points_uniform(92, n).astype(np.float32)
+    v, g, h = c.eval_multi(torch.from_numpy(pos).cuda(), vgh=True)
+    sub = np.r_[0:50, 65530:65545, n - 50:n]
+    ref = cpu_to_gpu_layout("s", *T.eval(pos[sub].astype(np.float64), sem=1))
+    got = (v.cpu().numpy()[sub], g.cpu().numpy()[sub].reshape(-1, 5, 3), h.cpu().numpy()[sub].reshape(-1, 5, 6))
+    assert_close(got, ref, TOL["s"], "70k points")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,N", [("s", 1), ("s", 33), ("c", 1), ("d", 3), ("z", 5)])
+def test_small_and_odd_spline_counts(orc, kind, N):
+    import torch
+    grids, bcs = [(0.0, 2.0, 7), (1.0, 2.0, 9), (-1.0, 0.0, 6)], [(P, P), (NA, FL), (AP, AP)]
+    G, T, _ = build_pair(orc, kind, grids, bcs, N, seed=93)
+    lo, hi = table_box(grids)
+    pos = synth.points_uniform(94, 123, lo, hi)
+    got = [x.cpu().numpy() for x in G.eval(torch.from_numpy(pos).cuda(), rule=0, layout=1)]
+    assert_close(got, T.eval(pos, sem=0), TOL[kind], f"{kind} N={N}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", "sd")
+def test_nonperiodic_table_through_cuda_entry(orc, kind):
+    """The reference's create_*_cuda assumes periodic tables
+    (src/multi_bspline_create_cuda.cu:449); here any boundary condition works,
+    with dim = cells per axis and the reference's clamp rule."""
+    import torch
+    grids = [(0.0, 1.5, 10), (0.0, 1.0, 8), (0.0, 2.0, 9)]
+    bcs = [(NA, NA), (D1, D2, 0.3, 0.0, -0.2, 0.0), (FL, FL)]
+    G, T, _ = build_pair(orc, kind, grids, bcs, 11, seed=95)
+    c = G.to_cuda()
+    assert (c.fields.dim.x, c.fields.dim.y, c.fields.dim.z) == (9, 7, 8)
+    pos = synth.points_uniform(96, 200, (0, 0, 0), (1.5, 1.0, 2.0))
+    f64 = kind == "d"
+    if not f64:
+        pos = pos.astype(np.float32).astype(np.float64)
+    dt = torch.float64 if f64 else torch.float32
+    v, g, h = c.eval_multi(torch.from_numpy(pos).to(dt).cuda(), vgh=True)
+    ref = cpu_to_gpu_layout(kind, *T.eval(pos, sem=1))
+    got = (v.cpu().numpy(), g.cpu().numpy().reshape(ref[1].shape), h.cpu().numpy().reshape(ref[2].shape))
+    assert_close(got, ref, TOL[kind], "non-periodic cuda entry")
+
+
+@pytest.mark.gpu
+def test_host_entry_with_strides(orc):
+    G, T, _ = build_pair(orc, "s", [(0.0, 1.0, 12)] * 3, [(P, P)] * 3, 9, seed=97)
+    pos = synth.points_uniform(98, 40)
+    vs, gs, hs = 13, 3 * 9 + 2, 6 * 9 + 1
+    v = np.full((40, vs), -5.0, np.float32)
+    g = np.full((40, gs), -5.0, np.float32)
+    h = np.full((40, hs), -5.0, np.float32)
+    o = L.EvalOpts(1, 1, 0, 0, 0, vs, gs, hs)
+    L.load().einspline_gb300_eval_3d_host(G.table, C.byref(o), 40, C.c_void_p(pos.ctypes.data),
+                                          C.c_void_p(v.ctypes.data), C.c_void_p(g.ctypes.data),
+                                          C.c_void_p(h.ctypes.data))
+    api.check()
+    ref = cpu_to_gpu_layout("s", *T.eval(pos, sem=0))
+    assert_close((v[:, :9], g[:, :27].reshape(40, 9, 3), h[:, :54].reshape(40, 9, 6)), ref, TOL["s"], "strided host")
+    assert (v[:, 9:] == -5).all() and (g[:, 27:] == -5).all() and (h[:, 54:] == -5).all()
+
+
+@pytest.mark.gpu
+def test_argument_errors_on_gpu():
+    lib = L.load()
+    G = api.MultiUBspline3D("s", [(0.0, 1.0, 8)] * 3, [(P, P)] * 3, 4)
+    with pytest.raises(api.EinsplineError, match="outside"):
+        G.set(4, np.zeros((8, 8, 8), np.float32))
+    with pytest.raises(api.EinsplineError, match="outside"):
+        G.set(-1, np.zeros((8, 8, 8), np.float32))
+    o = L.EvalOpts(1, 1, 0, 0, 0, 0, 0, 0)
+    rc = lib.einspline_gb300_eval_3d(G.table, C.byref(o), 10, None, None, None, None, None)
+    assert rc == 1 and b"NULL" in lib.einspline_gb300_last_error_message()
+    assert lib.einspline_gb300_set_tile(G.table, 48, 1, 1) == 1
+    assert lib.einspline_gb300_set_load_mode(G.table, 7) == 1
+    lib.einspline_gb300_clear_error()
+    with pytest.raises(ValueError):
+        api.MultiUBspline3D("d", [(0.0, 1.0, 8)] * 3, [(P, P)] * 3, 4, storage=api.STORE_F16)
