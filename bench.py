@@ -311,21 +311,32 @@ def run_gpu(args):
         hp = [torch.from_numpy(p).pin_memory() for p, _ in batches[:max(1, args.e2e_steps)]]
         ho = (torch.empty((maxp, NSPL), pin_memory=True), torch.empty((maxp, NSPL, 3), pin_memory=True),
               torch.empty((maxp, NSPL, 6), pin_memory=True))
-        for k in range(min(2, len(hp))):
-            P = hp[k].shape[0]
-            t.eval_host(hp[k].numpy(), out=(ho[0][:P].numpy(), ho[1][:P].numpy(), ho[2][:P].numpy()))
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ev, h2d, d2h = 0, 0, 0
-        for k in range(len(hp)):
-            P = hp[k].shape[0]
-            t.eval_host(hp[k].numpy(), out=(ho[0][:P].numpy(), ho[1][:P].numpy(), ho[2][:P].numpy()))
-            ev += P * NSPL
-            h2d += P * 24
-            d2h += P * NSPL * 10 * 4
-        el = time.perf_counter() - t0
-        e2e = {"value": ev / el * world, "unit": UNIT, "h2d_bytes_per_step": h2d // len(hp),
-               "d2h_bytes_per_step": d2h // len(hp), "path": "einspline_gb300_eval_3d_host (pinned host buffers)"}
+
+        def e2e_run(mode):
+            t.set_host_direct(mode)
+            for k in range(min(2, len(hp))):
+                P = hp[k].shape[0]
+                t.eval_host(hp[k].numpy(), out=(ho[0][:P].numpy(), ho[1][:P].numpy(), ho[2][:P].numpy()))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ev, h2d, d2h = 0, 0, 0
+            for k in range(len(hp)):
+                P = hp[k].shape[0]
+                t.eval_host(hp[k].numpy(), out=(ho[0][:P].numpy(), ho[1][:P].numpy(), ho[2][:P].numpy()))
+                ev += P * NSPL
+                h2d += P * 24
+                d2h += P * NSPL * 10 * 4
+            return ev / (time.perf_counter() - t0), h2d // len(hp), d2h // len(hp)
+
+        copy_rate, h2d, d2h = e2e_run(0)
+        direct_rate, _, _ = e2e_run(1)
+        t.set_host_direct(-1)
+        best = max(copy_rate, direct_rate)
+        e2e = {"value": best * world, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "path": "einspline_gb300_eval_3d_host, pinned host buffers; results written "
+                       + ("by the kernel into mapped host memory" if direct_rate >= copy_rate
+                          else "to device memory and copied back in overlapped chunks"),
+               "copy_pipeline_value": copy_rate * world, "direct_write_value": direct_rate * world}
 
     # serving: Poisson arrivals of single-walker requests replayed natively
     # through the request server (continuous batching, graph launches);

@@ -216,6 +216,10 @@ class MultiUBspline3D:
         check()
         return out
 
+    def set_host_direct(self, mode: int) -> None:
+        _lib().einspline_gb300_set_host_direct(self.table, int(mode))
+        check()
+
     def eval_host(self, pos: np.ndarray, vgh=True, rule=0, layout=0, out=None):
         """einspline_gb300_eval_3d_host: host numpy buffers (pin them for speed)."""
         P = pos.shape[0]

@@ -149,6 +149,24 @@ int einspline_gb300_eval_3d(einspline_gb300_table *t, const einspline_gb300_eval
   return eval_device(t, o, npts, pos_d, vals_d, grads_d, hess_d, s);
 }
 
+// Device address of a pinned, mapped host buffer, or NULL.
+static void *mapped_address(const void *h) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (at.type == cudaMemoryTypeHost && at.devicePointer) ? at.devicePointer : nullptr;
+}
+
+int einspline_gb300_set_host_direct(einspline_gb300_table *t, int mode) {
+  clear();
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (mode < -1 || mode > 1) return fail(EINSPLINE_GB300_EINVAL, "mode must be -1, 0 or 1");
+  t->host_direct = mode;
+  return 0;
+}
+
 int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300_eval_opts *o, int64_t npts,
                                  const void *pos_h, void *vals_h, void *grads_h, void *hess_h) {
   clear();
@@ -159,6 +177,21 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
     return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_eval_3d_host: NULL buffer");
   if (int r = table_flush(t)) return r;
   std::lock_guard<std::mutex> lock(t->mu);
+  if (t->host_direct != 0) {
+    // Pinned host buffers mapped into the device address space: one launch
+    // reads the positions and writes the results through NVLink-C2C / PCIe,
+    // with no staging copies.
+    void *pd = mapped_address(pos_h), *vd = mapped_address(vals_h);
+    void *gd = o->vgh ? mapped_address(grads_h) : nullptr, *hd = o->vgh ? mapped_address(hess_h) : nullptr;
+    if (pd && vd && (!o->vgh || (gd && hd))) {
+      cudaStream_t s = t->stream;
+      if (int r = eval_device(t, o, npts, pd, vd, gd, hd, s)) return r;
+      EG_CUDA(cudaStreamSynchronize(s));
+      return 0;
+    }
+    if (t->host_direct == 1)
+      return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_eval_3d_host: direct mode needs pinned, mapped buffers");
+  }
   const size_t rb = t->storage == ST_F64 ? 8 : 4;
   const int hq = o->layout ? 9 : 6;
   const size_t per_pt_out = (size_t)t->ncol * rb * (o->vgh ? (4 + hq) : 1);

@@ -97,3 +97,21 @@ def test_argument_errors_on_gpu():
     lib.einspline_gb300_clear_error()
     with pytest.raises(ValueError):
         api.MultiUBspline3D("d", [(0.0, 1.0, 8)] * 3, [(P, P)] * 3, 4, storage=api.STORE_F16)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [0, 1])
+def test_host_entry_copy_and_direct_modes_agree(orc, mode):
+    """Pinned buffers: results written by the kernel straight into mapped host
+    memory (mode 1) or staged through device memory (mode 0) are identical."""
+    import torch
+    G, T, _ = build_pair(orc, "s", [(0.0, 1.0, 12)] * 3, [(P, P)] * 3, 16, seed=99)
+    pos = torch.from_numpy(synth.points_uniform(100, 500)).pin_memory()
+    out = (torch.empty((500, 16), pin_memory=True), torch.empty((500, 16, 3), pin_memory=True),
+           torch.empty((500, 16, 6), pin_memory=True))
+    G.set_host_direct(mode)
+    got = G.eval_host(pos.numpy(), out=tuple(o.numpy() for o in out))
+    G.set_host_direct(-1)
+    ref = [x.cpu().numpy() for x in G.eval(pos.cuda(), rule=0, layout=0)]
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
