@@ -109,9 +109,9 @@ struct einspline_gb300_table {
   cudaStream_t pipe_stream[2] = {nullptr, nullptr};
   cudaEvent_t pipe_event[2] = {nullptr, nullptr};
 
-  // host-buffer entry: -1 automatic, 0 always copy through device memory,
-  // 1 kernels read/write pinned host buffers directly when they are mapped
-  int host_direct = -1;
+  // host-buffer entry: 0 copy through device memory (default), 1 kernels
+  // read/write mapped pinned host buffers directly
+  int host_direct = 0;
 
   // cell-sorted evaluation scratch
   void *sort_dev = nullptr;

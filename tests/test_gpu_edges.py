@@ -111,7 +111,7 @@ def test_host_entry_copy_and_direct_modes_agree(orc, mode):
            torch.empty((500, 16, 6), pin_memory=True))
     G.set_host_direct(mode)
     got = G.eval_host(pos.numpy(), out=tuple(o.numpy() for o in out))
-    G.set_host_direct(-1)
+    G.set_host_direct(0)
     ref = [x.cpu().numpy() for x in G.eval(pos.cuda(), rule=0, layout=0)]
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
