@@ -321,6 +321,7 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
     t->tile_mode = pf;
     for (int tx = 32; tx <= 256; tx *= 2) {
       if (tx > 32 && (tx / 2) * VW >= t->ncol) break;  // wider tiles only idle threads
+      if (pf == 3 && tx > 32) break;                   // the wide pipeline is one warp per block
       for (int ty = 1; tx * ty <= 256 && (pf < 2 || ty == 1); ty *= 2)
         for (int m = 1; m <= 8; m *= 2) {
           const int pb = ty * m;

@@ -87,9 +87,11 @@ __device__ __forceinline__ double fmaT(double a, double b, double c) { return fm
 
 // Cubic B-spline basis at offset t: w[0..3] values, w[4..7] first and
 // w[8..11] second derivatives (the 4x4 power-basis matrices of
-// src/bspline_data.c:143-162 in Horner form).
+// src/bspline_data.c:143-162 in Horner form).  The derivative rows carry the
+// axis' delta_inv (d) and delta_inv^2, so the reduction yields derivatives
+// in position units directly.
 template <typename A>
-__device__ __forceinline__ void bspline_weights(A t, A *w) {
+__device__ __forceinline__ void bspline_weights(A t, A *w, A d) {
   const A s6 = A(1) / A(6), t2 = t * t;
   w[0] = fmaT(fmaT(fmaT(-s6, t, A(0.5)), t, A(-0.5)), t, s6);
   w[1] = fmaT(fmaT(A(0.5), t, A(-1)), t2, A(2) / A(3));
@@ -103,6 +105,12 @@ __device__ __forceinline__ void bspline_weights(A t, A *w) {
   w[9] = fmaT(A(3), t, A(-2));
   w[10] = fmaT(A(-3), t, A(1));
   w[11] = t;
+  const A d2 = d * d;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    w[4 + i] *= d;
+    w[8 + i] *= d2;
+  }
 }
 
 // Cell index and offset along one axis.
@@ -275,16 +283,6 @@ __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col
 #pragma unroll
       for (int e = 0; e < VW; e++) o[q][e] *= (A)sc[e];
   }
-  if (VGH) {
-    A dx, dy, dz;
-    if (sizeof(A) == 4) { dx = (A)a.dinvf[0]; dy = (A)a.dinvf[1]; dz = (A)a.dinvf[2]; }
-    else { dx = (A)a.dinv[0]; dy = (A)a.dinv[1]; dz = (A)a.dinv[2]; }
-    const A f[10] = {A(1), dx, dy, dz, dx * dx, dx * dy, dx * dz, dy * dy, dy * dz, dz * dz};
-#pragma unroll
-    for (int q = 1; q < 10; q++)
-#pragma unroll
-      for (int e = 0; e < VW; e++) o[q][e] *= f[q];
-  }
   if (a.sign) {
     const A sg = reinterpret_cast<const A *>(a.sign)[src];
 #pragma unroll
@@ -446,7 +444,7 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
     int idx;
     A t;
     cell(a, ax, xd, idx, t);
-    bspline_weights<A>(t, sw + pp * 36 + ax * 12);
+    bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
     sidx[pp * 3 + ax] = idx;
     if (ax == 0) ssrc[pp] = src;
   }
@@ -498,7 +496,7 @@ __device__ __forceinline__ int eval_prologue(const EvalArgs &a, unsigned char *s
     int idx;
     A t;
     cell(a, ax, xd, idx, t);
-    bspline_weights<A>(t, sw + pp * 36 + ax * 12);
+    bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
     sidx[pp * 3 + ax] = idx;
     if (ax == 0) ssrc[pp] = src;
   }
@@ -534,7 +532,9 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tile = blockIdx.x % a.ntiles;
   const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
-  const int nthr = blockDim.x;
+  // The wide variant always runs one warp per block, which makes every
+  // shared-memory row offset below a compile-time constant.
+  const int nthr = WIDE ? 32 : blockDim.x;
   const int pn = eval_prologue<A>(a, smem, p0, threadIdx.x, nthr);
   __syncthreads();
   const A *sw = reinterpret_cast<const A *>(smem);
@@ -641,6 +641,10 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   const int VW = elems_per_thread(t) * (a.mode == 3 ? 2 : 1);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   *smem = smem_total(pb, acc_bytes(t));
+  if (a.mode == 3) {
+    tx = 32;  // the wide pipeline runs one warp per block
+    a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
+  }
   if (a.mode >= 2) {
     ty = 1;
     const int rb = (t->storage == ST_F32 || a.mode == 3) ? 16 : 8;
