@@ -118,6 +118,7 @@ def _signatures():
         sig[f"eval_multi_UBspline_3d_{k}_vgh"] = ([H, dbl, dbl, dbl, vp, vp, vp], None)
         sig[f"eval_multi_UBspline_3d_{k}_vg"] = ([H, dbl, dbl, dbl, vp, vp], None)
         sig[f"eval_multi_UBspline_3d_{k}_vgl"] = ([H, dbl, dbl, dbl, vp, vp, vp], None)
+        sig[f"eval_multi_UBspline_3d_{k}_vghgh"] = ([H, dbl, dbl, dbl, vp, vp, vp, vp], None)
         sig[f"eval_multi_multi_UBspline_3d_{k}_vgl_cuda"] = ([D, vp, vp, vp, vp, i32, i32], None)
         sig[f"create_multi_UBspline_3d_{k}_cuda"] = ([H], D)
         sig[f"destroy_multi_UBspline_3d_{k}_cuda"] = ([D], None)

@@ -186,6 +186,20 @@ class MultiUBspline3D:
         check()
         return v, g, lap
 
+    def eval_point_vghgh(self, x: float, y: float, z: float):
+        """eval_multi_UBspline_3d_*_vghgh: (vals, grads, hess[3][3],
+        gradhess[3][3][3]) at one point."""
+        dt = out_dtype(self.kind)
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((self.N,) + ext, dt)
+        g = np.zeros((self.N, 3) + ext, dt)
+        h = np.zeros((self.N, 3, 3) + ext, dt)
+        gh = np.zeros((self.N, 3, 3, 3) + ext, dt)
+        getattr(_lib(), f"eval_multi_UBspline_3d_{self.kind}_vghgh")(self.ptr, x, y, z, v.ctypes.data, g.ctypes.data,
+                                                                     h.ctypes.data, gh.ctypes.data)
+        check()
+        return v, g, h, gh
+
     def out_shapes(self, P, layout):
         ext = (2,) if self.ncomp == 2 else ()
         if layout == 0:

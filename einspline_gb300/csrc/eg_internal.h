@@ -24,7 +24,8 @@ constexpr int kI16Bias = 32768;
 // Records a status for the calling thread; aborts when abort mode is on.
 int fail(int code, const char *fmt, ...);
 void clear();
-// Checks a CUDA status; records and returns ECUDA on failure.
+// Records a failed CUDA status e (call it only when e != cudaSuccess) and
+// returns ECUDA.
 int cuda_check(cudaError_t e, const char *what);
 #define EG_CUDA(call)                                                  \
   do {                                                                 \
@@ -100,7 +101,7 @@ struct einspline_gb300_table {
   cudaStream_t stream = nullptr;
 
   // single-point entry scratch
-  void *pt_dev = nullptr;           // device, 13 * ncol output reals
+  void *pt_dev = nullptr;           // device, 40 * ncol output reals
   void *pt_host = nullptr;          // pinned host copy
 
   // host-buffer pipeline scratch (einspline_gb300_eval_3d_host)
@@ -165,6 +166,7 @@ struct EvalArgs {
   void *const *grads_pp;
   void *const *hess_pp;
   void *vals, *grads, *hess;
+  void *ghess;                // vghgh: third derivatives [N][27] (CPU layout)
   int64_t vstride, gstride, hstride;
   int layout;                 // 0 GPU layout, 1 CPU layout
   int is_complex;

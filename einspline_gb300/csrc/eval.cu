@@ -595,6 +595,161 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   }
 }
 
+// Index of third-derivative entry m (3x3x3 row-major, m = 9a + 3b + c) among
+// the ten distinct ones (xxx, xxy, xxz, xyy, xyz, xzz, yyy, yyz, yzz, zzz).
+__device__ __forceinline__ int g27to10(int m) {
+  int a = m / 9, b = (m / 3) % 3, c = m % 3, t;
+  if (a > b) { t = a; a = b; b = t; }
+  if (b > c) { t = b; b = c; c = t; }
+  if (a > b) { t = a; a = b; b = t; }
+  // sorted (a <= b <= c): rank among the 10 multisets in lexicographic order
+  return (a == 0) ? ((b == 0) ? c : (b == 1) ? 2 + c : 5) : (a == 1) ? ((b == 1) ? 5 + c : 8) : 9;
+}
+
+// Value, gradient, Hessian and third derivatives at one point
+// (eval_multi_UBspline_3d_*_vghgh, src/multi_bspline_eval_std_s_impl.h:866-1038),
+// CPU-entry cell rule and CPU layout.  The first ten outputs use exactly the
+// operations of the vgh reduction, so they equal the vgh entry's bit for bit;
+// the third derivatives add the constant rows {-1, 3, -3, 1} * delta_inv^3.
+template <int ST>
+__global__ void __launch_bounds__(128) k_eval_vghgh(const EvalArgs a) {
+  using A = typename CT<ST>::A;
+  constexpr int VW = CT<ST>::VW;
+  const int col0 = (blockIdx.x * blockDim.x + threadIdx.x) * VW;
+  if (col0 >= a.ncol) return;
+  A w[36], w3[3][4];
+  int idx[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ax++) {
+    A t;
+    cell(a, ax, a.inl[ax], idx[ax], t);
+    const A d = sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax];
+    bspline_weights<A>(t, w + 12 * ax, d);
+    const A d3 = (d * d) * d;
+    w3[ax][0] = -d3; w3[ax][1] = A(3) * d3; w3[ax][2] = A(-3) * d3; w3[ax][3] = d3;
+  }
+  A wz[3][4];
+  z_weights<A>(w, wz);
+  const int64_t xsb = a.xs * CT<ST>::BYTES, ysb = a.ys * CT<ST>::BYTES, zsb = a.zs * CT<ST>::BYTES;
+  const char *base = reinterpret_cast<const char *>(a.coefs) + (int64_t)col0 * CT<ST>::BYTES + idx[0] * xsb +
+                     idx[1] * ysb + idx[2] * zsb;
+  A o[20][VW];
+#pragma unroll
+  for (int q = 0; q < 20; q++)
+#pragma unroll
+    for (int e = 0; e < VW; e++) o[q][e] = A(0);
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    // y[0..5] as in reduce_plane; y[6..9] = b3c0, b2c1, b1c2, b0c3
+    A y[10][VW];
+#pragma unroll
+    for (int q = 0; q < 10; q++)
+#pragma unroll
+      for (int e = 0; e < VW; e++) y[q][e] = A(0);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      A c[4][VW];
+#pragma unroll
+      for (int k = 0; k < 4; k++) load_row<ST>(base + i * xsb + j * ysb + k * zsb, c[k]);
+      const A by = w[12 + j], dby = w[16 + j], d2by = w[20 + j], d3by = w3[1][j];
+#pragma unroll
+      for (int e = 0; e < VW; e++) {
+        A z0 = c[0][e] * wz[0][0];
+        z0 = fmaT(c[1][e], wz[0][1], z0);
+        z0 = fmaT(c[2][e], wz[0][2], z0);
+        z0 = fmaT(c[3][e], wz[0][3], z0);
+        A z1 = c[0][e] * wz[1][0];
+        z1 = fmaT(c[1][e], wz[1][1], z1);
+        z1 = fmaT(c[2][e], wz[1][2], z1);
+        z1 = fmaT(c[3][e], wz[1][3], z1);
+        A z2 = c[0][e] * wz[2][0];
+        z2 = fmaT(c[1][e], wz[2][1], z2);
+        z2 = fmaT(c[2][e], wz[2][2], z2);
+        z2 = fmaT(c[3][e], wz[2][3], z2);
+        A z3 = c[0][e] * w3[2][0];
+        z3 = fmaT(c[1][e], w3[2][1], z3);
+        z3 = fmaT(c[2][e], w3[2][2], z3);
+        z3 = fmaT(c[3][e], w3[2][3], z3);
+        y[0][e] = fmaT(by, z0, y[0][e]);
+        y[1][e] = fmaT(dby, z0, y[1][e]);
+        y[2][e] = fmaT(d2by, z0, y[2][e]);
+        y[3][e] = fmaT(by, z1, y[3][e]);
+        y[4][e] = fmaT(dby, z1, y[4][e]);
+        y[5][e] = fmaT(by, z2, y[5][e]);
+        y[6][e] = fmaT(d3by, z0, y[6][e]);
+        y[7][e] = fmaT(d2by, z1, y[7][e]);
+        y[8][e] = fmaT(dby, z2, y[8][e]);
+        y[9][e] = fmaT(by, z3, y[9][e]);
+      }
+    }
+    const A ax = w[i], dax = w[4 + i], d2ax = w[8 + i], d3ax = w3[0][i];
+#pragma unroll
+    for (int e = 0; e < VW; e++) {
+      o[0][e] = fmaT(ax, y[0][e], o[0][e]);
+      o[1][e] = fmaT(dax, y[0][e], o[1][e]);
+      o[2][e] = fmaT(ax, y[1][e], o[2][e]);
+      o[3][e] = fmaT(ax, y[3][e], o[3][e]);
+      o[4][e] = fmaT(d2ax, y[0][e], o[4][e]);
+      o[5][e] = fmaT(dax, y[1][e], o[5][e]);
+      o[6][e] = fmaT(dax, y[3][e], o[6][e]);
+      o[7][e] = fmaT(ax, y[2][e], o[7][e]);
+      o[8][e] = fmaT(ax, y[4][e], o[8][e]);
+      o[9][e] = fmaT(ax, y[5][e], o[9][e]);
+      o[10][e] = fmaT(d3ax, y[0][e], o[10][e]);  // xxx
+      o[11][e] = fmaT(d2ax, y[1][e], o[11][e]);  // xxy
+      o[12][e] = fmaT(d2ax, y[3][e], o[12][e]);  // xxz
+      o[13][e] = fmaT(dax, y[2][e], o[13][e]);   // xyy
+      o[14][e] = fmaT(dax, y[4][e], o[14][e]);   // xyz
+      o[15][e] = fmaT(dax, y[5][e], o[15][e]);   // xzz
+      o[16][e] = fmaT(ax, y[6][e], o[16][e]);    // yyy
+      o[17][e] = fmaT(ax, y[7][e], o[17][e]);    // yyz
+      o[18][e] = fmaT(ax, y[8][e], o[18][e]);    // yzz
+      o[19][e] = fmaT(ax, y[9][e], o[19][e]);    // zzz
+    }
+  }
+  if (a.scale) {
+#pragma unroll
+    for (int e = 0; e < VW; e++) {
+      const A sc = (A)a.scale[col0 + e];
+#pragma unroll
+      for (int q = 0; q < 20; q++) o[q][e] *= sc;
+    }
+  }
+  A *vp = (A *)a.vals, *gp = (A *)a.grads, *hp = (A *)a.hess, *tp = (A *)a.ghess;
+#pragma unroll
+  for (int e = 0; e < VW; e++) {
+    const int col = col0 + e;
+    if (col >= a.ncol) break;
+    // complex columns interleave re/im of one spline: element m of spline
+    // col/2 sits at 2m + (col & 1) within that spline's block
+    const int n = a.is_complex ? col >> 1 : col, p = a.is_complex ? col & 1 : 0, nc = a.is_complex ? 2 : 1;
+    vp[col] = o[0][e];
+#pragma unroll
+    for (int c = 0; c < 3; c++) gp[nc * (3 * n + c) + p] = o[1 + c][e];
+#pragma unroll
+    for (int m = 0; m < 9; m++) hp[nc * (9 * n + m) + p] = o[4 + h9to6(m)][e];
+#pragma unroll
+    for (int m = 0; m < 27; m++) tp[nc * (27 * n + m) + p] = o[10 + g27to10(m)][e];
+  }
+}
+
+int launch_vghgh(Table *t, const EvalArgs &a, cudaStream_t s) {
+  const int VW = elems_per_thread(t);
+  const int nthr = (a.ncol + VW - 1) / VW;
+  const int tx = nthr < 128 ? (nthr + 31) / 32 * 32 : 128;
+  const unsigned grid = (unsigned)((nthr + tx - 1) / tx);
+  switch (t->storage) {
+    case ST_F32: k_eval_vghgh<ST_F32><<<grid, tx, 0, s>>>(a); break;
+    case ST_F16: k_eval_vghgh<ST_F16><<<grid, tx, 0, s>>>(a); break;
+    case ST_BF16: k_eval_vghgh<ST_BF16><<<grid, tx, 0, s>>>(a); break;
+    case ST_I16: k_eval_vghgh<ST_I16><<<grid, tx, 0, s>>>(a); break;
+    default: k_eval_vghgh<ST_F64><<<grid, tx, 0, s>>>(a); break;
+  }
+  EG_CUDA(cudaGetLastError());
+  count_launch();
+  return 0;
+}
+
 void fill_eval_geometry(const Table *t, EvalArgs &a) {
   a.coefs = t->coefs;
   a.scale = t->scale;
@@ -736,6 +891,21 @@ Table *host_table(S *s, const char *fn) {
   return s->gb300;
 }
 
+// Device and pinned host scratch for the single-point entries: 40 output
+// reals per column (value, 3 gradient, 9 Hessian, 27 third-derivative).
+int point_scratch(Table *t, const char *fn) {
+  if (t->pt_dev) return 0;
+  const size_t sz = 40 * (size_t)t->ncol * acc_bytes(t);
+  if (cudaMalloc(&t->pt_dev, sz) != cudaSuccess || cudaMallocHost(&t->pt_host, sz) != cudaSuccess) {
+    cudaGetLastError();
+    if (t->pt_dev) cudaFree(t->pt_dev);
+    t->pt_dev = nullptr;
+    t->pt_host = nullptr;
+    return fail(EINSPLINE_GB300_ENOMEM, "%s: scratch allocation failed", fn);
+  }
+  return 0;
+}
+
 // Single point, host outputs in the CPU layout.  out: 0 vgh, 2 vgl, 3 vg.
 template <typename S, typename V>
 void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, bool vgh, const char *fn,
@@ -748,13 +918,7 @@ void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, 
   const size_t rb = acc_bytes(t);
   const size_t n = (size_t)t->ncol;
   const size_t bytes = (vgh ? 13 : 1) * n * rb;
-  if (!t->pt_dev) {
-    if (cudaMalloc(&t->pt_dev, 13 * n * rb) != cudaSuccess || cudaMallocHost(&t->pt_host, 13 * n * rb) != cudaSuccess) {
-      cudaGetLastError();
-      fail(EINSPLINE_GB300_ENOMEM, "%s: scratch allocation failed", fn);
-      return;
-    }
-  }
+  if (point_scratch(t, fn)) return;
   EvalArgs a;
   memset(&a, 0, sizeof(a));
   fill_eval_geometry(t, a);
@@ -782,6 +946,41 @@ void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, 
     if (out == 0) memcpy(hess, (char *)t->pt_host + 4 * n * rb, 9 * n * rb);
     if (out == 2) memcpy(hess, (char *)t->pt_host + 4 * n * rb, n * rb);
   }
+}
+
+// Single point value/gradient/Hessian/third derivatives, CPU layout.
+template <typename S, typename V>
+void eval_point_vghgh(S *s, double x, double y, double z, V *vals, V *grads, V *hess, V *gradhess, const char *fn) {
+  clear();
+  Table *t = host_table(s, fn);
+  if (!t) return;
+  if (!vals || !grads || !hess || !gradhess) { fail(EINSPLINE_GB300_EINVAL, "%s: NULL output", fn); return; }
+  if (table_flush(t)) return;
+  std::lock_guard<std::mutex> g(t->mu);
+  const size_t rb = acc_bytes(t);
+  const size_t n = (size_t)t->ncol;
+  if (point_scratch(t, fn)) return;
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  fill_eval_geometry(t, a);
+  a.inl[0] = x; a.inl[1] = y; a.inl[2] = z;
+  a.rule = 0;
+  a.layout = 1;
+  a.npts = 1;
+  a.vals = t->pt_dev;
+  a.grads = (char *)t->pt_dev + n * rb;
+  a.hess = (char *)t->pt_dev + 4 * n * rb;
+  a.ghess = (char *)t->pt_dev + 13 * n * rb;
+  if (launch_vghgh(t, a, t->stream)) return;
+  if (cudaMemcpyAsync(t->pt_host, t->pt_dev, 40 * n * rb, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
+      cudaStreamSynchronize(t->stream) != cudaSuccess) {
+    cuda_check(cudaGetLastError(), fn);
+    return;
+  }
+  memcpy(vals, t->pt_host, n * rb);
+  memcpy(grads, (char *)t->pt_host + n * rb, 3 * n * rb);
+  memcpy(hess, (char *)t->pt_host + 4 * n * rb, 9 * n * rb);
+  memcpy(gradhess, (char *)t->pt_host + 13 * n * rb, 27 * n * rb);
 }
 
 // Batched, reference GPU-entry semantics and layout, pointer-array outputs.
@@ -850,6 +1049,26 @@ void eval_multi_UBspline_3d_z_vgh(multi_UBspline_3d_z *s, double x, double y, do
                                   complex_double *grads, complex_double *hess) {
   eval_point<multi_UBspline_3d_z, complex_double>(s, x, y, z, vals, grads, hess, true,
                                                   "eval_multi_UBspline_3d_z_vgh");
+}
+
+// Third derivatives: src/multi_bspline_eval_std_s_impl.h:866,
+// src/multi_bspline_eval_std_d_impl.h:868, src/multi_bspline_eval_std_c_impl.h:864,
+// src/multi_bspline_eval_std_z_impl.h:868.
+void eval_multi_UBspline_3d_s_vghgh(multi_UBspline_3d_s *s, double x, double y, double z, float *vals, float *grads,
+                                    float *hess, float *gradhess) {
+  eval_point_vghgh(s, x, y, z, vals, grads, hess, gradhess, "eval_multi_UBspline_3d_s_vghgh");
+}
+void eval_multi_UBspline_3d_d_vghgh(multi_UBspline_3d_d *s, double x, double y, double z, double *vals,
+                                    double *grads, double *hess, double *gradhess) {
+  eval_point_vghgh(s, x, y, z, vals, grads, hess, gradhess, "eval_multi_UBspline_3d_d_vghgh");
+}
+void eval_multi_UBspline_3d_c_vghgh(multi_UBspline_3d_c *s, double x, double y, double z, complex_float *vals,
+                                    complex_float *grads, complex_float *hess, complex_float *gradhess) {
+  eval_point_vghgh(s, x, y, z, vals, grads, hess, gradhess, "eval_multi_UBspline_3d_c_vghgh");
+}
+void eval_multi_UBspline_3d_z_vghgh(multi_UBspline_3d_z *s, double x, double y, double z, complex_double *vals,
+                                    complex_double *grads, complex_double *hess, complex_double *gradhess) {
+  eval_point_vghgh(s, x, y, z, vals, grads, hess, gradhess, "eval_multi_UBspline_3d_z_vghgh");
 }
 
 void eval_multi_UBspline_3d_s_vg(multi_UBspline_3d_s *s, double x, double y, double z, float *vals, float *grads) {

@@ -2,7 +2,8 @@
  * multi_bspline_eval_c.h -- single-point evaluation of a uniform 3D
  * multi-spline of type c (complex_float), host output buffers.
  *
- * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_c.h:92-115.
+ * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_c.h:92-115
+ * and the std backend's vghgh entry.
  * Output layout is the reference CPU layout: vals[N], grads[N][3],
  * hess[N][3][3] (full symmetric matrix, row-major).  The point may be given
  * anywhere; the reference reads outside its table when a point leaves
@@ -32,6 +33,12 @@ void eval_multi_UBspline_3d_c_vgl(multi_UBspline_3d_c *spline, double x, double 
 
 void eval_multi_UBspline_3d_c_vgh(multi_UBspline_3d_c *spline, double x, double y, double z,
                                    complex_float *vals, complex_float *grads, complex_float *hess);
+
+/* src/multi_bspline_eval_std_c_impl.h:864 (the reference declares it in its
+ * std/sse backend headers only): value, gradient, Hessian and third
+ * derivatives, gradhess[N][3][3][3] (all 27 entries, symmetric copies filled). */
+void eval_multi_UBspline_3d_c_vghgh(multi_UBspline_3d_c *spline, double x, double y, double z,
+                                     complex_float *vals, complex_float *grads, complex_float *hess, complex_float *gradhess);
 
 #ifdef __cplusplus
 }

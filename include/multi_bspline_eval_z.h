@@ -2,7 +2,8 @@
  * multi_bspline_eval_z.h -- single-point evaluation of a uniform 3D
  * multi-spline of type z (complex_double), host output buffers.
  *
- * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_z.h:87-110.
+ * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_z.h:87-110
+ * and the std backend's vghgh entry.
  * Output layout is the reference CPU layout: vals[N], grads[N][3],
  * hess[N][3][3] (full symmetric matrix, row-major).  The point may be given
  * anywhere; the reference reads outside its table when a point leaves
@@ -32,6 +33,12 @@ void eval_multi_UBspline_3d_z_vgl(multi_UBspline_3d_z *spline, double x, double 
 
 void eval_multi_UBspline_3d_z_vgh(multi_UBspline_3d_z *spline, double x, double y, double z,
                                    complex_double *vals, complex_double *grads, complex_double *hess);
+
+/* src/multi_bspline_eval_std_z_impl.h:868 (the reference declares it in its
+ * std/sse backend headers only): value, gradient, Hessian and third
+ * derivatives, gradhess[N][3][3][3] (all 27 entries, symmetric copies filled). */
+void eval_multi_UBspline_3d_z_vghgh(multi_UBspline_3d_z *spline, double x, double y, double z,
+                                     complex_double *vals, complex_double *grads, complex_double *hess, complex_double *gradhess);
 
 #ifdef __cplusplus
 }

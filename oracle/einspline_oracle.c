@@ -11,7 +11,7 @@
  * baseline).  The GPU library never links or calls it.
  *
  * Pinning: tests/test_oracle.py compares this code bit for bit against the
- * reference's own CPU sources (compiled by oracle/build_ref.sh when the
+ * reference's own CPU sources (compiled by `make -C oracle ref` when the
  * reference tree is present) and against the committed golden vectors in
  * tests/golden/, which were produced by that compiled reference.
  *
@@ -423,6 +423,118 @@ void orc_eval_z(const orc_desc *d, int sem, int vgh, const double *coefs, double
 {
   enum { NC = 2 };
   ORC_EVAL_BODY(double, cell_d, basis_d)
+}
+
+/* Value, gradient, Hessian and third derivatives ("vghgh"): the reference's
+ * eval_multi_UBspline_3d_{s,d,c,z}_vghgh (src/multi_bspline_eval_std_s_impl.h:866-1038,
+ * _d_impl.h:868, _c_impl.h:864, _z_impl.h), declared in its backend headers
+ * (src/multi_bspline_eval_std_s.h etc.).  gradhess is [N][3][3][3]; the ten
+ * distinct entries are accumulated and copied to their symmetric places. */
+#define ORC_VGHGH_BODY(REAL, CELL, BASIS)                                         \
+  const int N = d->num_splines;                                                   \
+  int ix, iy, iz; REAL tx, ty, tz;                                                \
+  CELL(&d->ax[0], 0, x, &ix, &tx);                                                \
+  CELL(&d->ax[1], 0, y, &iy, &ty);                                                \
+  CELL(&d->ax[2], 0, z, &iz, &tz);                                                \
+  REAL wa[3][4], wb[3][4], wc[3][4];                                              \
+  BASIS(tx, wa); BASIS(ty, wb); BASIS(tz, wc);                                    \
+  const REAL d3w[4] = {(REAL)-1.0, (REAL)3.0, (REAL)-3.0, (REAL)1.0};             \
+  const int64_t xs = NC * d->xs, ys = NC * d->ys, zs = NC * d->zs;                \
+  for (int n = 0; n < NC * N; n++) vals[n] = 0;                                   \
+  for (int n = 0; n < 3 * NC * N; n++) grads[n] = 0;                              \
+  for (int n = 0; n < 9 * NC * N; n++) hess[n] = 0;                               \
+  for (int n = 0; n < 27 * NC * N; n++) gh[n] = 0;                                \
+  static const int gpos[10] = {0, 1, 2, 4, 5, 8, 13, 14, 17, 26};                 \
+  for (int i = 0; i < 4; i++)                                                     \
+    for (int j = 0; j < 4; j++)                                                   \
+      for (int k = 0; k < 4; k++) {                                               \
+        const REAL *cf = coefs + (ix+i)*xs + (iy+j)*ys + (iz+k)*zs;               \
+        REAL w[20];                                                               \
+        w[0] = wa[0][i]*wb[0][j]*wc[0][k];                                        \
+        w[1] = wa[1][i]*wb[0][j]*wc[0][k];                                        \
+        w[2] = wa[0][i]*wb[1][j]*wc[0][k];                                        \
+        w[3] = wa[0][i]*wb[0][j]*wc[1][k];                                        \
+        w[4] = wa[2][i]*wb[0][j]*wc[0][k];                                        \
+        w[5] = wa[1][i]*wb[1][j]*wc[0][k];                                        \
+        w[6] = wa[1][i]*wb[0][j]*wc[1][k];                                        \
+        w[7] = wa[0][i]*wb[2][j]*wc[0][k];                                        \
+        w[8] = wa[0][i]*wb[1][j]*wc[1][k];                                        \
+        w[9] = wa[0][i]*wb[0][j]*wc[2][k];                                        \
+        w[10] = d3w[i]*wb[0][j]*wc[0][k];                                         \
+        w[11] = wa[2][i]*wb[1][j]*wc[0][k];                                       \
+        w[12] = wa[2][i]*wb[0][j]*wc[1][k];                                       \
+        w[13] = wa[1][i]*wb[2][j]*wc[0][k];                                       \
+        w[14] = wa[1][i]*wb[1][j]*wc[1][k];                                       \
+        w[15] = wa[1][i]*wb[0][j]*wc[2][k];                                       \
+        w[16] = wa[0][i]*d3w[j]*wc[0][k];                                         \
+        w[17] = wa[0][i]*wb[2][j]*wc[1][k];                                       \
+        w[18] = wa[0][i]*wb[1][j]*wc[2][k];                                       \
+        w[19] = wa[0][i]*wb[0][j]*d3w[k];                                         \
+        for (int n = 0; n < N; n++)                                               \
+          for (int p = 0; p < NC; p++) {                                          \
+            REAL cv = cf[NC*n + p];                                               \
+            vals[NC*n + p] += w[0] * cv;                                          \
+            for (int c = 0; c < 3; c++) grads[NC*(3*n+c) + p] += w[1+c] * cv;     \
+            hess[NC*(9*n+0) + p] += w[4] * cv;                                    \
+            hess[NC*(9*n+1) + p] += w[5] * cv;                                    \
+            hess[NC*(9*n+2) + p] += w[6] * cv;                                    \
+            hess[NC*(9*n+4) + p] += w[7] * cv;                                    \
+            hess[NC*(9*n+5) + p] += w[8] * cv;                                    \
+            hess[NC*(9*n+8) + p] += w[9] * cv;                                    \
+            for (int m = 0; m < 10; m++) gh[NC*(27*n+gpos[m]) + p] += w[10+m] * cv; \
+          }                                                                       \
+      }                                                                           \
+  REAL dx = (REAL)d->ax[0].delta_inv, dy = (REAL)d->ax[1].delta_inv;              \
+  REAL dz = (REAL)d->ax[2].delta_inv;                                             \
+  const REAL f3[10] = {dx*dx*dx, dx*dx*dy, dx*dx*dz, dx*dy*dy, dx*dy*dz,          \
+                       dx*dz*dz, dy*dy*dy, dy*dy*dz, dy*dz*dz, dz*dz*dz};         \
+  /* symmetric copies: for each distinct entry, the other index orders */        \
+  static const int copies[10][6] = {{-1}, {3, 9, -1}, {6, 18, -1}, {10, 12, -1},  \
+      {7, 11, 15, 19, 21, -1}, {20, 24, -1}, {-1}, {16, 22, -1}, {23, 25, -1}, {-1}}; \
+  for (int n = 0; n < N; n++)                                                     \
+    for (int p = 0; p < NC; p++) {                                                \
+      grads[NC*(3*n+0)+p] *= dx;                                                  \
+      grads[NC*(3*n+1)+p] *= dy;                                                  \
+      grads[NC*(3*n+2)+p] *= dz;                                                  \
+      hess[NC*(9*n+0)+p] *= dx*dx;                                                \
+      hess[NC*(9*n+4)+p] *= dy*dy;                                                \
+      hess[NC*(9*n+8)+p] *= dz*dz;                                                \
+      hess[NC*(9*n+1)+p] *= dx*dy;                                                \
+      hess[NC*(9*n+2)+p] *= dx*dz;                                                \
+      hess[NC*(9*n+5)+p] *= dy*dz;                                                \
+      hess[NC*(9*n+3)+p] = hess[NC*(9*n+1)+p];                                    \
+      hess[NC*(9*n+6)+p] = hess[NC*(9*n+2)+p];                                    \
+      hess[NC*(9*n+7)+p] = hess[NC*(9*n+5)+p];                                    \
+      for (int m = 0; m < 10; m++) {                                              \
+        REAL *g0 = &gh[NC*(27*n+gpos[m])+p];                                      \
+        *g0 *= f3[m];                                                             \
+        for (int c = 0; c < 6 && copies[m][c] >= 0; c++) gh[NC*(27*n+copies[m][c])+p] = *g0; \
+      }                                                                           \
+    }
+
+void orc_eval_s_vghgh(const orc_desc *d, const float *coefs, double x, double y, double z,
+                      float *vals, float *grads, float *hess, float *gh)
+{
+  enum { NC = 1 };
+  ORC_VGHGH_BODY(float, cell_f, basis_f)
+}
+void orc_eval_d_vghgh(const orc_desc *d, const double *coefs, double x, double y, double z,
+                      double *vals, double *grads, double *hess, double *gh)
+{
+  enum { NC = 1 };
+  ORC_VGHGH_BODY(double, cell_d, basis_d)
+}
+void orc_eval_c_vghgh(const orc_desc *d, const float *coefs, double x, double y, double z,
+                      float *vals, float *grads, float *hess, float *gh)
+{
+  enum { NC = 2 };
+  ORC_VGHGH_BODY(float, cell_f, basis_f)
+}
+void orc_eval_z_vghgh(const orc_desc *d, const double *coefs, double x, double y, double z,
+                      double *vals, double *grads, double *hess, double *gh)
+{
+  enum { NC = 2 };
+  ORC_VGHGH_BODY(double, cell_d, basis_d)
 }
 
 /* Many points, OpenMP over points as the reference's timing driver does

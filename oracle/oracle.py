@@ -61,6 +61,10 @@ def lib(fast: bool = False) -> C.CDLL:
             f = getattr(L, "orc_eval_" + t)
             f.argtypes = [C.POINTER(OrcDesc), C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double,
                           C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+        for t in "sdcz":
+            f = getattr(L, f"orc_eval_{t}_vghgh")
+            f.argtypes = [C.POINTER(OrcDesc), C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                          C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_eval_batch.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(OrcDesc), C.c_void_p,
                                      C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_eval_batch.restype = C.c_int
@@ -121,6 +125,15 @@ class Table:
             self._coefs = np.ascontiguousarray(self.coefs64.astype(self.dtype))
         return self._coefs
 
+    def eval_vghgh(self, pos: np.ndarray, coefs: np.ndarray = None):
+        """Value, gradient, Hessian and third derivatives [P][N][3][3][3]
+        (CPU-entry rule), as eval_multi_UBspline_3d_*_vghgh."""
+        cf = self.coefs if coefs is None else np.ascontiguousarray(coefs)
+        f = getattr(lib(), f"orc_eval_{self.kind}_vghgh")
+        return _vghgh(lambda o, c, x, y, z, v, g, h, gh: f(C.byref(o), ptr(c), x, y, z, ptr(v), ptr(g), ptr(h),
+                                                           ptr(gh)),
+                      self.desc, pos, self.dtype, self.N, self.ncomp, cf)
+
     def eval(self, pos: np.ndarray, vgh: bool = True, sem: int = 0, coefs: np.ndarray = None,
              nthreads: int = 0, fast: bool = False):
         """Evaluate at pos (npts,3).  sem=0: CPU-entry semantics; sem=1: the
@@ -137,6 +150,19 @@ class Table:
         lib(fast).orc_eval_batch(ord(self.kind), sem, int(vgh), C.byref(self.desc), ptr(cf), P,
                                  ptr(pos), ptr(v), ptr(g), ptr(h), nthreads)
         return v, g, h
+
+
+def _vghgh(fn, obj, pos, dtype, N, ncomp, coefs):
+    pos = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    P = pos.shape[0]
+    ext = (2,) if ncomp == 2 else ()
+    v = np.zeros((P, N) + ext, dtype)
+    g = np.zeros((P, N, 3) + ext, dtype)
+    h = np.zeros((P, N, 3, 3) + ext, dtype)
+    gh = np.zeros((P, N, 3, 3, 3) + ext, dtype)
+    for p in range(P):
+        fn(obj, coefs, *[float(c) for c in pos[p]], v[p], g[p], h[p], gh[p])
+    return v, g, h, gh
 
 
 def _as_pairs(data, ncomp):
@@ -208,6 +234,8 @@ def ref_lib() -> C.CDLL:
                                                                      C.c_double, C.c_void_p]
             getattr(_ref, f"eval_multi_UBspline_3d_{t}_vgh").argtypes = [
                 C.POINTER(S), C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+            getattr(_ref, f"eval_multi_UBspline_3d_{t}_vghgh").argtypes = [
+                C.POINTER(S), C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _ref.destroy_Bspline.argtypes = [C.c_void_p]
     return _ref
 
@@ -279,6 +307,11 @@ class RefSpline:
             else:
                 fv(self.p, x, y, z, ptr(v[p]))
         return (v, g, h) if vgh else (v, None, None)
+
+    def eval_vghgh(self, pos):
+        f = getattr(ref_lib(), f"eval_multi_UBspline_3d_{self.kind}_vghgh")
+        return _vghgh(lambda o, c, x, y, z, v, g, h, gh: f(o, x, y, z, ptr(v), ptr(g), ptr(h), ptr(gh)),
+                      self.p, pos, self.dtype, self.N, self.ncomp, None)
 
     def __del__(self):
         try:

@@ -1,10 +1,11 @@
 """The other epilogues of the same gather: the reference GPU entries' sign
 and vgl (lattice-transformed gradient and laplacian) forms, and the CPU
-entries' vg and vgl forms, against the oracle's vgh on the same table."""
+entries' vg, vgl and vghgh (third derivatives) forms, against the oracle
+on the same table."""
 import numpy as np
 import pytest
 
-from einspline_gb300 import synth
+from einspline_gb300 import api, synth
 
 from helpers import TOL, assert_close, build_pair, rel_err, table_box
 
@@ -96,3 +97,47 @@ def test_cpu_vg_vgl(orc, kind):
         assert np.array_equal(v2, v) and np.array_equal(g2, g)
         rl = rh[:, 0, 0] + rh[:, 1, 1] + rh[:, 2, 2]
         assert rel_err(lap, rl) <= 4 * TOL[kind]
+
+
+def _sym_ok(gh):
+    """gh [N][3][3][3] (complex: trailing re/im axis) is symmetric in its
+    three derivative indices."""
+    for perm in [(0, 2, 1, 3), (0, 1, 3, 2), (0, 3, 2, 1)]:
+        if not np.array_equal(gh, np.transpose(gh, perm + tuple(range(4, gh.ndim)))):
+            return False
+    return True
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", "sdcz")
+def test_cpu_vghgh(orc, kind):
+    """eval_multi_UBspline_3d_*_vghgh: value/gradient/Hessian equal the vgh
+    entry bit for bit; third derivatives match the oracle (which is pinned to
+    the reference's std backend) within the type's tolerance."""
+    for grids, bcs in ((PERIODIC_UNIT, [(P, P)] * 3), MIXED):
+        G, T, _ = build_pair(orc, kind, grids, bcs, 9, seed=88)
+        lo, hi = table_box(grids)
+        for p in synth.points_uniform(89, 5, lo, hi):
+            v, g, h, gh = G.eval_point_vghgh(*p)
+            v0, g0, h0 = G.eval_point(*p, vgh=True)
+            assert np.array_equal(v, v0) and np.array_equal(g, g0) and np.array_equal(h, h0)
+            rv, rg, rh, rgh = (x[0] for x in T.eval_vghgh(p[None]))
+            assert_close((v, g, h), (rv, rg, rh), TOL[kind], "vghgh")
+            e = rel_err(gh, rgh)
+            assert e <= TOL[kind], f"third derivatives: rel err {e:.3e}"
+            assert _sym_ok(gh)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16, api.STORE_I16])
+def test_cpu_vghgh_16bit(orc, storage):
+    """16-bit tables: the same entry against the oracle on the dequantized table."""
+    grids, bcs = MIXED
+    G, T, _ = build_pair(orc, "s", grids, bcs, 12, seed=90, storage=storage)
+    tab = np.ascontiguousarray(G.table_values().astype(np.float32))
+    lo, hi = table_box(grids)
+    for p in synth.points_uniform(91, 4, lo, hi):
+        got = G.eval_point_vghgh(*p)
+        ref = [x[0] for x in T.eval_vghgh(p[None], coefs=tab)]
+        for a, b in zip(got, ref):
+            assert rel_err(a, b) <= TOL["s"]

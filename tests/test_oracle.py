@@ -81,3 +81,28 @@ def test_live_reference(orc, kind):
             for x, y in zip(a, b):
                 if x is not None:
                     assert np.array_equal(x, y)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref",
+                                                    "libeinspline_ref.so")),
+                    reason="reference library not built here (make -C oracle ref)")
+@pytest.mark.parametrize("kind", "sdcz")
+def test_live_reference_vghgh(orc, kind):
+    """Third derivatives (eval_multi_UBspline_3d_*_vghgh of the std backend),
+    bit for bit on the reference's own table."""
+    from einspline_gb300 import synth
+    P, NA, D1, D2, FL, AP = orc.PERIODIC, orc.NATURAL, orc.DERIV1, orc.DERIV2, orc.FLAT, orc.ANTIPERIODIC
+    cases = [([(0.0, 1.3, 7), (-0.5, 0.7, 9), (0.1, 1.0, 6)], [(P, P)] * 3),
+             ([(0.0, 1.3, 7), (-0.5, 0.7, 9), (0.1, 1.0, 6)],
+              [(NA, D1, 0.0, 0.0, 0.3, -0.2), (D2, FL, 0.5, 0.1, 0.0, 0.0), (AP, AP)])]
+    for grids, bcs in cases:
+        N = 5
+        T = orc.Table(kind, grids, bcs, N)
+        R = orc.RefSpline(kind, grids, bcs, N)
+        data = synth.grid_data_uniform(78, T.M, N, np.float64, complex_=kind in "cz")
+        for i in range(N):
+            R.set_spline(i, data[i])
+        tab = np.ascontiguousarray(R.table())
+        pos = synth.points_uniform(6, 24, [g[0] for g in grids], [g[1] for g in grids])
+        for x, y in zip(T.eval_vghgh(pos, coefs=tab), R.eval_vghgh(pos)):
+            assert np.array_equal(x, y)
