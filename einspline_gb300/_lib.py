@@ -86,6 +86,11 @@ class EvalOpts(C.Structure):
                 ("sort", C.c_int), ("vstride", C.c_int64), ("gstride", C.c_int64), ("hstride", C.c_int64)]
 
 
+class DetOpts(C.Structure):
+    _fields_ = [("nelec", C.c_int), ("k", C.c_int), ("ld", C.c_int), ("ainv_trans", C.c_int),
+                ("pos_f64", C.c_int), ("rule", C.c_int)]
+
+
 class TableInfo(C.Structure):
     _fields_ = [("kind", C.c_int), ("storage", C.c_int), ("num_splines", C.c_int), ("ncol", C.c_int),
                 ("ncol_pad", C.c_int), ("elem_bytes", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
@@ -158,6 +163,8 @@ def _signatures():
     sig["einspline_gb300_get_load_mode"] = ([vp], i32)
     sig["einspline_gb300_launch_count"] = ([], i64)
     sig["einspline_gb300_fill_uniform"] = ([vp, i64, i32, C.c_uint64, i64, dbl, dbl, vp], i32)
+    sig["einspline_gb300_det_ratio"] = ([vp, C.POINTER(DetOpts), i32, vp, vp, vp, vp, vp, vp, vp], i32)
+    sig["einspline_gb300_det_update"] = ([C.POINTER(DetOpts), i32, vp, vp, vp, vp, vp], i32)
     sig["einspline_gb300_server_create"] = ([vp, C.POINTER(ServerOpts)], vp)
     sig["einspline_gb300_server_destroy"] = ([vp], i32)
     sig["einspline_gb300_server_submit"] = ([vp, vp, i32], i64)

@@ -452,6 +452,69 @@ class Server:
             pass
 
 
+class Determinants:
+    """A population of walkers' Slater matrices A [W][ld][ld] and inverses
+    (torch float32 CUDA tensors, one contiguous block each) for the fused
+    determinant step: einspline_gb300_det_ratio / _det_update.  trans=0 keeps
+    Ainv[j][e] (orbital j, electron e) as the reference does; trans=1 stores
+    its transpose so column k is contiguous."""
+
+    def __init__(self, A, ainv, nelec: int, trans: int = 0):
+        torch = _torch()
+        self.A, self.ainv = A, ainv
+        self.W, self.ld = int(A.shape[0]), int(A.shape[-1])
+        self.nelec, self.trans = int(nelec), int(trans)
+        self.a_ptrs = self._ptrs(A)
+        self.ainv_ptrs = self._ptrs(ainv)
+        self.work = torch.empty(2 * self.nelec * self.W, dtype=torch.float32, device=A.device)
+
+    @staticmethod
+    def _ptrs(t):
+        torch = _torch()
+        step = t[0].numel() * t.element_size()
+        return torch.tensor([t.data_ptr() + i * step for i in range(t.shape[0])], dtype=torch.int64,
+                            device=t.device)
+
+    def opts(self, k, pos_f64=False, rule=1):
+        return L.DetOpts(self.nelec, int(k), self.ld, self.trans, int(pos_f64), int(rule))
+
+    def ratio(self, spline: "MultiUBspline3D", pos, k: int, grad_lapl=True, rows=None, rule=1, stream=None):
+        """Ratios (and gradient / Laplacian ratios) of every walker moving
+        electron k to pos [W, 3]; rows: optional [W, >= nelec] float32 tensor
+        that receives the new orbital rows."""
+        torch = _torch()
+        W = int(pos.shape[0])
+        dev = pos.device
+        ratio = torch.empty(W, dtype=torch.float32, device=dev)
+        grad = torch.empty(W, 3, dtype=torch.float32, device=dev) if grad_lapl else None
+        lapl = torch.empty(W, dtype=torch.float32, device=dev) if grad_lapl else None
+        row_ptrs = self._ptrs(rows) if rows is not None else None
+        o = self.opts(k, pos.dtype == torch.float64, rule)
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)  # noqa: E731
+        s = C.c_void_p(stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream)
+        _lib().einspline_gb300_det_ratio(spline.table, C.byref(o), W, ptr(pos), ptr(self.ainv_ptrs), ptr(ratio),
+                                         ptr(grad), ptr(lapl), ptr(row_ptrs), s)
+        check()
+        return ratio, grad, lapl
+
+    def update(self, k: int, accepted, rows, stream=None):
+        """Sherman-Morrison update of the accepted walkers (indices) whose
+        row k becomes rows[i] (rows: [W, >= nelec] float32 CUDA tensor)."""
+        torch = _torch()
+        idx = torch.as_tensor(accepted, dtype=torch.int64, device=self.A.device)
+        n = int(idx.numel())
+        if n == 0:
+            return
+        a = self.a_ptrs[idx].contiguous()
+        ai = self.ainv_ptrs[idx].contiguous()
+        r = self._ptrs(rows)[idx].contiguous()
+        o = self.opts(k)
+        s = C.c_void_p(stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream)
+        _lib().einspline_gb300_det_update(C.byref(o), n, C.c_void_p(a.data_ptr()), C.c_void_p(ai.data_ptr()),
+                                          C.c_void_p(r.data_ptr()), C.c_void_p(self.work.data_ptr()), s)
+        check()
+
+
 def launch_count() -> int:
     return int(_lib().einspline_gb300_launch_count())
 

@@ -1,0 +1,239 @@
+// Device building blocks shared by the evaluation kernels (eval.cu) and the
+// fused determinant kernels (det.cu): coefficient storage types, the cubic
+// B-spline basis, the two cell rules and the separable 4x4x4 reduction.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "eg_internal.h"
+
+namespace eg {
+
+// ------------------------------------------------------------ coefficient types
+// Raw is what one thread reads per stencil row (VW stored reals); decode
+// turns it into VW accumulator values.
+template <int ST> struct CT;
+template <> struct CT<ST_F32> {
+  using A = float;
+  using Raw = float4;
+  static constexpr int VW = 4, BYTES = 4;
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
+    v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+  }
+};
+template <> struct CT<ST_F16> {
+  using A = float;
+  using Raw = uint2;
+  static constexpr int VW = 4, BYTES = 2;
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
+    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&x.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&x.y));
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+};
+template <> struct CT<ST_BF16> {
+  using A = float;
+  using Raw = uint2;
+  static constexpr int VW = 4, BYTES = 2;
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
+    v[0] = __uint_as_float(x.x << 16); v[1] = __uint_as_float(x.x & 0xFFFF0000u);
+    v[2] = __uint_as_float(x.y << 16); v[3] = __uint_as_float(x.y & 0xFFFF0000u);
+  }
+};
+template <> struct CT<ST_I16> {
+  using A = float;
+  using Raw = uint2;
+  static constexpr int VW = 4, BYTES = 2;
+  // A biased 16-bit pattern u placed under the exponent of 2^23 is the float
+  // 2^23 + u; subtracting 2^23 + bias is exact and leaves the integer.
+  __device__ static __forceinline__ void decode(const Raw &x, float (&v)[4]) {
+    const float off = 8388608.0f + (float)kI16Bias;
+    v[0] = __int_as_float(__byte_perm(x.x, 0x4B000000u, 0x7610)) - off;
+    v[1] = __int_as_float(__byte_perm(x.x, 0x4B000000u, 0x7632)) - off;
+    v[2] = __int_as_float(__byte_perm(x.y, 0x4B000000u, 0x7610)) - off;
+    v[3] = __int_as_float(__byte_perm(x.y, 0x4B000000u, 0x7632)) - off;
+  }
+};
+template <> struct CT<ST_F64> {
+  using A = double;
+  using Raw = double2;
+  static constexpr int VW = 2, BYTES = 8;
+  __device__ static __forceinline__ void decode(const Raw &x, double (&v)[2]) { v[0] = x.x; v[1] = x.y; }
+};
+
+template <int ST>
+__device__ __forceinline__ void load_row(const char *p, typename CT<ST>::A (&v)[CT<ST>::VW]) {
+  CT<ST>::decode(__ldg(reinterpret_cast<const typename CT<ST>::Raw *>(p)), v);
+}
+
+
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+
+// Cubic B-spline basis at offset t: w[0..3] values, w[4..7] first and
+// w[8..11] second derivatives (the 4x4 power-basis matrices of
+// src/bspline_data.c:143-162 in Horner form).  The derivative rows carry the
+// axis' delta_inv (d) and delta_inv^2, so the reduction yields derivatives
+// in position units directly.
+template <typename A>
+__device__ __forceinline__ void bspline_weights(A t, A *w, A d) {
+  const A s6 = A(1) / A(6), t2 = t * t;
+  w[0] = fmaT(fmaT(fmaT(-s6, t, A(0.5)), t, A(-0.5)), t, s6);
+  w[1] = fmaT(fmaT(A(0.5), t, A(-1)), t2, A(2) / A(3));
+  w[2] = fmaT(fmaT(fmaT(A(-0.5), t, A(0.5)), t, A(0.5)), t, s6);
+  w[3] = s6 * t2 * t;
+  w[4] = fmaT(fmaT(A(-0.5), t, A(1)), t, A(-0.5));
+  w[5] = fmaT(A(1.5), t, A(-2)) * t;
+  w[6] = fmaT(fmaT(A(-1.5), t, A(1)), t, A(0.5));
+  w[7] = A(0.5) * t2;
+  w[8] = A(1) - t;
+  w[9] = fmaT(A(3), t, A(-2));
+  w[10] = fmaT(A(-3), t, A(1));
+  w[11] = t;
+  const A d2 = d * d;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    w[4 + i] *= d;
+    w[8 + i] *= d2;
+  }
+}
+
+// Cell index and offset along one axis.
+//  rule 0 (CPU entries, src/multi_bspline_eval_std_s_impl.h:746-755):
+//    u = (x - start) * delta_inv, rounded to float for FP32 tables;
+//    i = trunc(u), t = u - i (modf).  Outside the table the edge cell is
+//    extrapolated (the reference reads out of bounds there).
+//  rule 1 (GPU entries, src/multi_bspline_cuda_s_impl.h:370-384):
+//    u = r * delta_inv (no start offset), i = clamp(floor(u), 0, dim-1),
+//    t = u - floor(u).
+__device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &idx, float &t) {
+  const int lim = a.lim[ax];
+  if (a.rule == 0) {
+    const float u = __double2float_rn(__dmul_rn(__dsub_rn(xd, a.start[ax]), a.dinv[ax]));
+    const float ip = truncf(u);
+    float tt = __fsub_rn(u, ip);
+    int i = (int)ip;
+    if (i < 0) { tt = __fadd_rn(tt, (float)i); i = 0; }
+    if (i > lim) { tt = __fadd_rn(tt, (float)(i - lim)); i = lim; }
+    idx = i; t = tt;
+  } else {
+    const float s = __fmul_rn((float)xd, a.dinvf[ax]);
+    const float sf = floorf(s);
+    int i = (int)sf;
+    i = i < 0 ? 0 : (i > lim ? lim : i);
+    idx = i; t = __fsub_rn(s, sf);
+  }
+}
+__device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &idx, double &t) {
+  const int lim = a.lim[ax];
+  if (a.rule == 0) {
+    const double u = __dmul_rn(__dsub_rn(xd, a.start[ax]), a.dinv[ax]);
+    const double ip = trunc(u);
+    double tt = __dsub_rn(u, ip);
+    int i = (int)ip;
+    if (i < 0) { tt = __dadd_rn(tt, (double)i); i = 0; }
+    if (i > lim) { tt = __dadd_rn(tt, (double)(i - lim)); i = lim; }
+    idx = i; t = tt;
+  } else {
+    const double s = __dmul_rn(xd, a.dinv[ax]);
+    const double sf = floor(s);
+    int i = (int)sf;
+    i = i < 0 ? 0 : (i > lim ? lim : i);
+    idx = i; t = __dsub_rn(s, sf);
+  }
+}
+
+// Separable reduction of the 4x4x4 stencil for VW columns.
+// w: [0..11] x weights, [12..23] y weights, [24..35] z weights.
+// o: v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz.
+// One x-plane i: rows (i, j, k) come from row(j, k, c); z first, then y,
+// then this plane's x terms are added to o.
+template <typename A, int VW, bool VGH, typename RowFn>
+__device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3][4], RowFn row, A (&o)[10][VW]) {
+  A y[6][VW];
+#pragma unroll
+  for (int q = 0; q < 6; q++)
+#pragma unroll
+    for (int e = 0; e < VW; e++) y[q][e] = A(0);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    A c[4][VW];
+#pragma unroll
+    for (int k = 0; k < 4; k++) row(j, k, c[k]);
+    const A by = w[12 + j], dby = w[16 + j], d2by = w[20 + j];
+#pragma unroll
+    for (int e = 0; e < VW; e++) {
+      A z0 = c[0][e] * wz[0][0];
+      z0 = fmaT(c[1][e], wz[0][1], z0);
+      z0 = fmaT(c[2][e], wz[0][2], z0);
+      z0 = fmaT(c[3][e], wz[0][3], z0);
+      y[0][e] = fmaT(by, z0, y[0][e]);
+      if (VGH) {
+        A z1 = c[0][e] * wz[1][0];
+        z1 = fmaT(c[1][e], wz[1][1], z1);
+        z1 = fmaT(c[2][e], wz[1][2], z1);
+        z1 = fmaT(c[3][e], wz[1][3], z1);
+        A z2 = c[0][e] * wz[2][0];
+        z2 = fmaT(c[1][e], wz[2][1], z2);
+        z2 = fmaT(c[2][e], wz[2][2], z2);
+        z2 = fmaT(c[3][e], wz[2][3], z2);
+        y[1][e] = fmaT(dby, z0, y[1][e]);
+        y[2][e] = fmaT(d2by, z0, y[2][e]);
+        y[3][e] = fmaT(by, z1, y[3][e]);
+        y[4][e] = fmaT(dby, z1, y[4][e]);
+        y[5][e] = fmaT(by, z2, y[5][e]);
+      }
+    }
+  }
+  const A ax = w[i], dax = w[4 + i], d2ax = w[8 + i];
+#pragma unroll
+  for (int e = 0; e < VW; e++) {
+    o[0][e] = fmaT(ax, y[0][e], o[0][e]);
+    if (VGH) {
+      o[1][e] = fmaT(dax, y[0][e], o[1][e]);
+      o[2][e] = fmaT(ax, y[1][e], o[2][e]);
+      o[3][e] = fmaT(ax, y[3][e], o[3][e]);
+      o[4][e] = fmaT(d2ax, y[0][e], o[4][e]);
+      o[5][e] = fmaT(dax, y[1][e], o[5][e]);
+      o[6][e] = fmaT(dax, y[3][e], o[6][e]);
+      o[7][e] = fmaT(ax, y[2][e], o[7][e]);
+      o[8][e] = fmaT(ax, y[4][e], o[8][e]);
+      o[9][e] = fmaT(ax, y[5][e], o[9][e]);
+    }
+  }
+}
+
+template <typename A, int VW>
+__device__ __forceinline__ void zero_out(A (&o)[10][VW]) {
+#pragma unroll
+  for (int q = 0; q < 10; q++)
+#pragma unroll
+    for (int e = 0; e < VW; e++) o[q][e] = A(0);
+}
+
+template <typename A>
+__device__ __forceinline__ void z_weights(const A *w, A (&wz)[3][4]) {
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+#pragma unroll
+    for (int k = 0; k < 4; k++) wz[d][k] = w[24 + 4 * d + k];
+}
+
+// All four planes, rows read straight from global memory.
+template <int ST, bool VGH>
+__device__ __forceinline__ void contract(const char *base, int64_t xsb, int64_t ysb, int64_t zsb,
+                                         const typename CT<ST>::A *w, typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
+  using A = typename CT<ST>::A;
+  constexpr int VW = CT<ST>::VW;
+  zero_out<A, VW>(o);
+  A wz[3][4];
+  z_weights<A>(w, wz);
+#pragma unroll 1
+  for (int i = 0; i < 4; i++) {
+    const char *plane = base + i * xsb;
+    reduce_plane<A, VW, VGH>(i, w, wz, [&](int j, int k, A(&c)[VW]) { load_row<ST>(plane + j * ysb + k * zsb, c); },
+                             o);
+  }
+}
+
+}  // namespace eg

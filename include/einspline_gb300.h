@@ -240,6 +240,52 @@ int einspline_gb300_server_replay(einspline_gb300_server *s, int nreq, const dou
                                   const int *npts, const int64_t *offsets, const void *pos_host,
                                   double *latency_s, double *wall_s);
 
+/* ------------------------------------------------- QMC determinant step
+ * The consumer of the orbital row in the reference's QMC prototype
+ * (src/cuda_walker.cu): every walker moves electron k; the N orbitals are
+ * evaluated at its new position (calc_new_row, :69-88), dotted with column k
+ * of the walker's inverse Slater matrix (calc_ratios, :171-201) and, when the
+ * move is accepted, the inverse gets a Sherman-Morrison update
+ * (update_inverse_cuda1/2, src/determinant_update.h:9-111, launched at
+ * src/cuda_walker.cu:92-136).  No single reference entry point corresponds:
+ * these replace that kernel sequence.  Real float tables only (s kind, any
+ * float or 16-bit storage); A and Ainv are float. */
+typedef struct {
+  int nelec;       /* N: determinant size, orbitals 0..N-1 of the table      */
+  int k;           /* the moved electron: row k of A, column k of Ainv       */
+  int ld;          /* leading dimension of every A and Ainv, floats (>= N)   */
+  int ainv_trans;  /* 0: Ainv[j*ld + e] (orbital j, electron e), the
+                      reference's layout, column k strided in memory;
+                      1: the transpose, Ainv[e*ld + j]: column k contiguous,
+                      fewer bytes per ratio.  A is always A[e*ld + j].      */
+  int pos_f64;     /* positions double (1) or float (0), xyz interleaved     */
+  int rule;        /* cell rule, as in einspline_gb300_eval_opts             */
+} einspline_gb300_det_opts;
+
+/* For each of nwalkers walkers w (all buffers in device memory; ainv_d and
+ * row_d are device arrays of device pointers, one per walker):
+ *   ratio_d[w]    = sum_j phi_j(r_w) Ainv_w[j][k]
+ *   grad_d[3w..]  = sum_j grad phi_j(r_w) Ainv_w[j][k] / ratio   (optional)
+ *   lapl_d[w]     = sum_j lapl phi_j(r_w) Ainv_w[j][k] / ratio   (optional)
+ *   row_d[w][j]   = phi_j(r_w), j < N                           (optional)
+ * with r_w = pos_d[3w..3w+2].  The orbital values, gradients and Laplacians
+ * are never written to memory (except the value row when row_d != NULL); the
+ * row equals einspline_gb300_eval_3d's values bit for bit.  Sums run in a
+ * fixed order, so results do not vary from run to run.  Asynchronous on
+ * stream (NULL = legacy default stream). */
+int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_det_opts *opts, int nwalkers,
+                              const void *pos_d, const float *const *ainv_d, float *ratio_d,
+                              float *grad_d, float *lapl_d, float *const *row_d, void *stream);
+
+/* Sherman-Morrison update of naccept walkers' inverses after row k of A is
+ * replaced by row_d[w] (device pointer arrays, as above):
+ *   x    = (u - A[k,:]) Ainv,   Ainv -= Ainv[:,k] x / (1 + x[k]),
+ *   A[k,:] = u.
+ * work_d: device scratch of 2 * nelec * naccept floats.  At most 65535
+ * walkers per call.  Asynchronous on stream. */
+int einspline_gb300_det_update(const einspline_gb300_det_opts *opts, int naccept, float *const *a_d,
+                               float *const *ainv_d, const float *const *row_d, float *work_d, void *stream);
+
 /* Kernel launches (and graph launches) this library has issued so far. */
 int64_t einspline_gb300_launch_count(void);
 

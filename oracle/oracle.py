@@ -318,3 +318,56 @@ class RefSpline:
             ref_lib().destroy_Bspline(C.cast(self.p, C.c_void_p))
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- determinant step
+# Restatement, in float64 numpy, of the reference QMC prototype's use of the
+# orbital row (src/cuda_walker.cu): the ratio of calc_ratios (:171-201),
+# ratio = sum_j u_j Ainv[j][k], and the two update kernels
+# update_inverse_cuda1/2 (src/determinant_update.h:9-111):
+#   x[c]   = sum_j Ainv[j][c] (u_j - A[k][j])          (kernel 1, :39-56)
+#   Ainv[j][c] += x[c] * (-1/(1 + x[k])) * Ainv[j][k]   (kernel 2, :86-108)
+#   A[k][:] = u                                         (kernel 1, :41-43)
+# Ainv is indexed [orbital j][electron c]; A is [electron][orbital].
+
+def det_ratio(vals, grads, hess, ainv, k):
+    """Per walker: ratio, (sum_j grad_j Ainv[j][k]) / ratio, (sum_j lapl_j
+    Ainv[j][k]) / ratio.  vals [W][N], grads [W][N][3], hess [W][N][3][3]
+    (CPU layout, oracle eval), ainv [W][N][N] as Ainv[j][c]."""
+    v = np.asarray(vals, np.float64)
+    col = np.asarray(ainv, np.float64)[:, :, k]
+    r = np.einsum("wj,wj->w", v, col)
+    out = [r, None, None]
+    if grads is not None:
+        g = np.einsum("wjd,wj->wd", np.asarray(grads, np.float64), col)
+        h = np.asarray(hess, np.float64)
+        lap = h[..., 0, 0] + h[..., 1, 1] + h[..., 2, 2]
+        out[1] = g / r[:, None]
+        out[2] = np.einsum("wj,wj->w", lap, col) / r
+    return out
+
+
+def det_ratio_bound(vals, grads, hess, ainv, k):
+    """sum_j |term_j| of each sum in det_ratio: the scale a rounding error of
+    the dot products is measured against."""
+    v = np.abs(np.asarray(vals, np.float64))
+    col = np.abs(np.asarray(ainv, np.float64)[:, :, k])
+    sr = np.einsum("wj,wj->w", v, col)
+    if grads is None:
+        return sr, None, None
+    sg = np.einsum("wjd,wj->wd", np.abs(np.asarray(grads, np.float64)), col)
+    h = np.asarray(hess, np.float64)
+    sl = np.einsum("wj,wj->w", np.abs(h[..., 0, 0] + h[..., 1, 1] + h[..., 2, 2]), col)
+    return sr, sg, sl
+
+
+def sm_update(A, ainv, k, u):
+    """Sherman-Morrison row update of one walker in float64: returns (A', Ainv')."""
+    A = np.array(A, np.float64)
+    Ai = np.array(ainv, np.float64)
+    u = np.asarray(u, np.float64)
+    x = (u - A[k]) @ Ai
+    colk = Ai[:, k].copy()
+    Ai += np.outer(colk, x) * (-1.0 / (1.0 + x[k]))
+    A[k] = u
+    return A, Ai

@@ -106,3 +106,17 @@ def test_live_reference_vghgh(orc, kind):
         pos = synth.points_uniform(6, 24, [g[0] for g in grids], [g[1] for g in grids])
         for x, y in zip(T.eval_vghgh(pos, coefs=tab), R.eval_vghgh(pos)):
             assert np.array_equal(x, y)
+
+
+def test_det_oracle_algebra(orc):
+    """The determinant-step restatement is the textbook algebra: the ratio is
+    det(A')/det(A) and the Sherman-Morrison update is inv(A')."""
+    rng = np.random.default_rng(5)
+    N, k = 24, 9
+    A = rng.standard_normal((N, N)) + 5 * np.eye(N)
+    Ai = np.linalg.inv(A)
+    u = rng.standard_normal(N)
+    A2, Ai2 = orc.sm_update(A, Ai, k, u)
+    assert np.abs(Ai2 - np.linalg.inv(A2)).max() <= 1e-12 * np.abs(Ai2).max()
+    r, _, _ = orc.det_ratio(u[None], None, None, Ai[None], k)
+    assert abs(r[0] - np.linalg.det(A2) / np.linalg.det(A)) <= 1e-12 * abs(r[0])
