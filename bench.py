@@ -372,6 +372,7 @@ def run_gpu(args):
     if rank == 0 and args.error_points > 0:
         err = precision_report(tabs, args.error_points)
     other = other_configs(args) if (rank == 0 and args.configs) else None
+    det = det_step(tabs) if (rank == 0 and args.det) else None
 
     if rank != 0:
         return
@@ -404,6 +405,7 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "error_vs_fp64": err,
         "other_configs": other,
+        "det_step": det,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -442,6 +444,84 @@ def precision_report(tabs, npts):
     rep["note"] = (f"{npts} points x {len(cols)} sampled splines vs eval_multi_UBspline_3d_d on the FP64 table; "
                    "max and rms of |error| / max |quantity|, and rel_l2 = ||error|| / ||quantity||")
     return rep
+
+
+def det_step(tabs, W=2048, reps=20):
+    """The fused QMC determinant step on the headline table (1024 orbitals,
+    N = 1024 electrons of one spin, W walkers each moving electron k):
+    einspline_gb300_det_ratio value-only and with gradient/Laplacian, both
+    Ainv layouts, against the unfused path (flat evaluation of the orbital
+    row into HBM, then a torch dot with the Ainv column), and the
+    Sherman-Morrison update of W/2 accepted walkers.  A and Ainv hold seeded
+    uniform values: the timing does not depend on them."""
+    import torch
+    from einspline_gb300 import api, synth
+    N = NSPL
+    A = torch.empty((W, N, N), dtype=torch.float32, device="cuda")
+    Ai = torch.empty_like(A)
+    api.fill_uniform(A, 91, -1.0, 1.0)
+    api.fill_uniform(Ai, 92, -1.0, 1.0)
+    pos = [torch.from_numpy(synth.points_uniform(93 + i, W).astype(np.float32)).cuda() for i in range(reps + 3)]
+    rows = torch.empty((W, N), dtype=torch.float32, device="cuda")
+    k = 17
+
+    def timeit(fn):
+        for i in range(3):
+            fn(pos[i])
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for i in range(reps):
+            fn(pos[3 + i])
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = {"walkers": W, "nelec": N, "orbitals": NSPL, "k": k}
+    for name in ("f16", "f32"):
+        t = tabs[name]
+        coef_b = 2 if name == "f16" else 4
+        res = {}
+        for trans in (1, 0):
+            D = api.Determinants(A, Ai, N, trans=trans)
+            ms_v = timeit(lambda p: D.ratio(t, p, k, grad_lapl=False))
+            ms_gl = timeit(lambda p: D.ratio(t, p, k, grad_lapl=True))
+            ms_row = timeit(lambda p: D.ratio(t, p, k, grad_lapl=True, rows=rows))
+            alg = 64 * coef_b + 4          # coefficients + one Ainv entry per orbital
+            res[f"trans{trans}"] = {
+                "ratio_ms": ms_v, "ratio_grad_lapl_ms": ms_gl, "ratio_grad_lapl_row_ms": ms_row,
+                "orbital_evals_per_s_grad_lapl": W * N / (ms_gl / 1e3),
+                "GBps_alg_grad_lapl": W * N * alg / (ms_gl / 1e3) / 1e9}
+        colk = Ai[:, :, k]                  # reference layout column, strided
+        vals = torch.empty((W, N), device="cuda")
+        gr = torch.empty((W, N, 3), device="cuda")
+        hs = torch.empty((W, N, 6), device="cuda")
+
+        def unfused_v(p):
+            t.eval(p, vgh=False, rule=1, out=(vals, None, None))
+            return (vals * colk).sum(-1)
+
+        def unfused_vgh(p):
+            t.eval(p, vgh=True, rule=1, out=(vals, gr, hs))
+            r = (vals * colk).sum(-1)
+            g = (gr * colk[:, :, None]).sum(1) / r[:, None]
+            lap = ((hs[:, :, 0] + hs[:, :, 3] + hs[:, :, 5]) * colk).sum(-1) / r
+            return r, g, lap
+        res["unfused_ratio_ms"] = timeit(unfused_v)
+        res["unfused_ratio_grad_lapl_ms"] = timeit(unfused_vgh)
+        res["speedup_grad_lapl_vs_unfused"] = res["unfused_ratio_grad_lapl_ms"] / res["trans1"]["ratio_grad_lapl_ms"]
+        out[name] = res
+        del vals, gr, hs
+    # update of half the walkers (3 N^2 floats of traffic each: read in pass 1,
+    # read + write in pass 2)
+    D = api.Determinants(A, Ai, N, trans=1)
+    acc = list(range(0, W, 2))
+    D.ratio(tabs["f16"], pos[0], k, grad_lapl=False, rows=rows)
+    ms_u = timeit(lambda p: D.update(k, acc, rows))
+    out["update"] = {"accepted": len(acc), "ms": ms_u, "GBps_alg": len(acc) * 3 * N * N * 4 / (ms_u / 1e3) / 1e9}
+    del A, Ai, D
+    torch.cuda.empty_cache()
+    return out
 
 
 def other_configs(args):
@@ -518,7 +598,8 @@ def main():
     ap.add_argument("--load", type=float, nargs="*", default=[0.5, 0.9])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--error-points", type=int, default=256)
-    ap.add_argument("--configs", type=int, default=0, help="also time the other BASELINE configurations")
+    ap.add_argument("--configs", type=int, default=0, help="also time the FP64, complex and 128^3 workloads")
+    ap.add_argument("--det", type=int, default=1, help="also time the fused determinant step")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -462,18 +462,31 @@ class Determinants:
     def __init__(self, A, ainv, nelec: int, trans: int = 0):
         torch = _torch()
         self.A, self.ainv = A, ainv
-        self.W, self.ld = int(A.shape[0]), int(A.shape[-1])
+        self.W, self.ld = int(A.shape[0]), int(ainv.shape[-1])
         self.nelec, self.trans = int(nelec), int(trans)
+        self._cache = {}
         self.a_ptrs = self._ptrs(A)
         self.ainv_ptrs = self._ptrs(ainv)
         self.work = torch.empty(2 * self.nelec * self.W, dtype=torch.float32, device=A.device)
 
-    @staticmethod
-    def _ptrs(t):
+    def _ptrs(self, t):
+        """Device array of per-walker pointers into t [W, ...] (cached)."""
         torch = _torch()
-        step = t[0].numel() * t.element_size()
-        return torch.tensor([t.data_ptr() + i * step for i in range(t.shape[0])], dtype=torch.int64,
-                            device=t.device)
+        key = ("p", t.data_ptr(), tuple(t.shape), tuple(t.stride()))
+        if key not in self._cache:
+            step = t.stride(0) * t.element_size()
+            base = torch.arange(t.shape[0], dtype=torch.int64, device=t.device) * step
+            self._cache[key] = base + t.data_ptr()
+        return self._cache[key]
+
+    def _index(self, accepted):
+        torch = _torch()
+        if isinstance(accepted, torch.Tensor):
+            return accepted.to(device=self.A.device, dtype=torch.int64)
+        key = ("i", tuple(int(i) for i in accepted))
+        if key not in self._cache:
+            self._cache[key] = torch.as_tensor(key[1], dtype=torch.int64, device=self.A.device)
+        return self._cache[key]
 
     def opts(self, k, pos_f64=False, rule=1):
         return L.DetOpts(self.nelec, int(k), self.ld, self.trans, int(pos_f64), int(rule))
@@ -501,7 +514,7 @@ class Determinants:
         """Sherman-Morrison update of the accepted walkers (indices) whose
         row k becomes rows[i] (rows: [W, >= nelec] float32 CUDA tensor)."""
         torch = _torch()
-        idx = torch.as_tensor(accepted, dtype=torch.int64, device=self.A.device)
+        idx = self._index(accepted)
         n = int(idx.numel())
         if n == 0:
             return

@@ -46,84 +46,185 @@ __device__ __forceinline__ float ainv_at(const float *m, int j, int c, int ld, i
   return trans ? m[(int64_t)c * ld + j] : m[(int64_t)j * ld + c];
 }
 
-template <int ST, bool GL>
-__global__ void __launch_bounds__(kDetThreads, 3) k_det_ratio(const DetArgs d) {
-  constexpr int VW = CT<ST>::VW;
+// Shared memory of k_det_ratio: the evaluation prologue's weights, cells and
+// sources for pb walkers, the copy pipeline, and per-warp partial sums.
+__host__ __device__ __forceinline__ size_t det_pipe_off(int pb) { return align_up(smem_total(pb, 4), 16); }
+__host__ __device__ __forceinline__ size_t det_red_off(int pb, int rb) {
+  return det_pipe_off(pb) + pipe_bytes(kDetThreads, rb);
+}
+__host__ __device__ __forceinline__ size_t det_ptr_off(int pb, int rb) {
+  return align_up(det_red_off(pb, rb) + (size_t)pb * (kDetThreads / 32) * 5 * sizeof(float), 16);
+}
+__host__ __device__ __forceinline__ size_t det_av_off(int pb, int rb) {
+  return align_up(det_ptr_off(pb, rb) + (size_t)pb * sizeof(void *), 16);
+}
+__host__ __device__ __forceinline__ size_t det_smem(int pb, int rb) {
+  return det_av_off(pb, rb) + (size_t)kDetThreads * 8 * sizeof(float);
+}
+
+// A block takes pb walkers and all N orbitals, in column groups of
+// kDetThreads * VW.  A pipeline stage is one x-plane (16 stencil rows) of one
+// column group of one walker; as in k_eval_pipe each thread copies its own
+// columns of the rows of stage s+2 into shared memory while it reduces stage
+// s, and reads back only what it copied.  At the end of a walker's planes the
+// thread dots its columns' value, gradient and Laplacian with the inverse
+// column (loaded when the walker's first plane starts, so its latency hides
+// behind the reduction); at the end of the walker each warp folds its lanes
+// with a fixed shuffle tree into shared memory, and after the loop one thread
+// per walker adds the warps in order.  WIDE (16-bit tables): 8 columns and
+// one 16-byte copy per thread and row.
+template <int ST, bool GL, bool WIDE>
+__global__ void __launch_bounds__(kDetThreads) k_det_ratio(const DetArgs d) {
+  using Raw = typename CT<ST>::Raw;
   static_assert(sizeof(typename CT<ST>::A) == 4, "determinant step: real float tables only");
-  __shared__ float sw[36];
-  __shared__ int sidx[3];
-  __shared__ float red[kDetThreads / 32][5];
+  constexpr int VW = WIDE ? 2 * CT<ST>::VW : CT<ST>::VW;
+  constexpr int RB = WIDE ? 2 * (int)sizeof(Raw) : (int)sizeof(Raw);
+  constexpr int NW = kDetThreads / 32;
+  extern __shared__ __align__(16) unsigned char smem[];
   const EvalArgs &a = d.e;
-  const int w = blockIdx.x;
-  if (threadIdx.x < 3) {
-    const int ax = threadIdx.x;
-    const double xd = a.pos_f64 ? reinterpret_cast<const double *>(a.pos)[3 * (int64_t)w + ax]
-                                : (double)reinterpret_cast<const float *>(a.pos)[3 * (int64_t)w + ax];
-    int idx;
-    float t;
-    cell(a, ax, xd, idx, t);
-    bspline_weights<float>(t, sw + 12 * ax, a.dinvf[ax]);
-    sidx[ax] = idx;
-  }
+  const int64_t p0 = (int64_t)blockIdx.x * a.pb;
+  const int pn = eval_prologue<float>(a, smem, p0, threadIdx.x, kDetThreads);
+  const float **sptr = reinterpret_cast<const float **>(smem + det_ptr_off(a.pb, RB));
+  for (int q = threadIdx.x; q < pn; q += kDetThreads) sptr[q] = d.ainv[p0 + q];
   __syncthreads();
-  const float *ainv = d.ainv[w];
-  float *row = d.row_out ? d.row_out[w] : nullptr;
+  const float *sw = reinterpret_cast<const float *>(smem);
+  const int *sidx = reinterpret_cast<const int *>(smem + smem_w_bytes(a.pb, 4));
+  const int64_t *ssrc = reinterpret_cast<const int64_t *>(smem + smem_w_bytes(a.pb, 4) + align_up((size_t)a.pb * 12, 8));
+  unsigned char *pipe = smem + det_pipe_off(a.pb);
+  float *red = reinterpret_cast<float *>(smem + det_red_off(a.pb, RB));
+  // the thread's inverse-column entries of the walker in flight: copied with
+  // the walker's first plane, read when that plane is reduced (the next
+  // first plane is four stages later, after the pipeline's depth)
+  float *avbuf = reinterpret_cast<float *>(smem + det_av_off(a.pb, RB)) + threadIdx.x * VW;
+
+  constexpr int GC = kDetThreads * VW;  // columns per group
+  const int G = (d.n + GC - 1) / GC;
   const int64_t xsb = a.xs * CT<ST>::BYTES, ysb = a.ys * CT<ST>::BYTES, zsb = a.zs * CT<ST>::BYTES;
-  const char *base = reinterpret_cast<const char *>(a.coefs) + sidx[0] * xsb + sidx[1] * ysb + sidx[2] * zsb;
-  float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-  for (int col0 = threadIdx.x * VW; col0 < d.n; col0 += kDetThreads * VW) {
-    float o[10][VW];
-    contract<ST, GL>(base + (int64_t)col0 * CT<ST>::BYTES, xsb, ysb, zsb, sw, o);
-    if (a.scale) {
+  const char *cbase = reinterpret_cast<const char *>(a.coefs) + (int64_t)threadIdx.x * VW * CT<ST>::BYTES;
+  const unsigned my = (unsigned)__cvta_generic_to_shared(pipe + (size_t)threadIdx.x * RB);
+  constexpr unsigned row_step = (unsigned)(kDetThreads * RB), slot_step = 16u * row_step;
+  const int S = pn * G * 4;
+  auto issue = [&](int st) {
+    const int i = st & 3, rest = st >> 2, g = rest % G, pp = rest / G;
+    if ((g * kDetThreads + (int)threadIdx.x) * VW >= d.n) return;
+    const char *plane = cbase + (int64_t)g * GC * CT<ST>::BYTES + (sidx[3 * pp] + i) * xsb +
+                        sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
+    const unsigned dst = my + (unsigned)(st % kPipeStages) * slot_step;
 #pragma unroll
-      for (int e = 0; e < VW; e++) {
-        const float sc = a.scale[col0 + e];
+    for (int r = 0; r < 16; r++) cp_async<RB>(dst + r * row_step, plane + (r >> 2) * ysb + (r & 3) * zsb);
+    if (i == 0) {
+      const int col0 = (g * kDetThreads + (int)threadIdx.x) * VW;
+      const float *src = d.trans ? sptr[pp] + (int64_t)d.k * d.ld + col0 : sptr[pp] + (int64_t)col0 * d.ld + d.k;
+      const unsigned av = (unsigned)__cvta_generic_to_shared(avbuf);
+      if (d.trans && col0 + VW <= d.n && al16(src)) {
 #pragma unroll
-        for (int q = 0; q < (GL ? 10 : 1); q++) o[q][e] *= sc;
+        for (int e = 0; e < VW; e += 4) cp_async<16>(av + 4 * e, reinterpret_cast<const char *>(src + e));
+      } else {
+        const int64_t step = d.trans ? 1 : d.ld;
+#pragma unroll
+        for (int e = 0; e < VW; e++)
+          if (col0 + e < d.n) cp_async<4>(av + 4 * e, reinterpret_cast<const char *>(src + e * step));
       }
     }
+  };
 #pragma unroll
-    for (int e = 0; e < VW; e++) {
-      const int j = col0 + e;
-      if (j >= d.n) break;
-      const float c = ainv_at(ainv, j, d.k, d.ld, d.trans);
-      acc[0] = fmaf(o[0][e], c, acc[0]);
-      if (GL) {
-        acc[1] = fmaf(o[1][e], c, acc[1]);
-        acc[2] = fmaf(o[2][e], c, acc[2]);
-        acc[3] = fmaf(o[3][e], c, acc[3]);
-        acc[4] = fmaf((o[4][e] + o[7][e]) + o[9][e], c, acc[4]);
+  for (int st = 0; st < kPipeStages - 1; st++) {
+    if (st < S) issue(st);
+    cp_async_commit();
+  }
+  float o[10][VW];
+  zero_out<float, VW>(o);
+  float wz[3][4];
+  float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float av[VW];
+  for (int st = 0; st < S; st++) {
+    if (st + kPipeStages - 1 < S) issue(st + kPipeStages - 1);
+    cp_async_commit();
+    cp_async_wait<kPipeStages - 1>();
+    const int i = st & 3, rest = st >> 2, g = rest % G, pp = rest / G;
+    const int col0 = (g * kDetThreads + (int)threadIdx.x) * VW;
+    const bool live = col0 < d.n;
+    const float *w = sw + pp * 36;
+    if (i == 0) {
+      z_weights<float>(w, wz);
+      if (live) {
+#pragma unroll
+        for (int e = 0; e < VW; e++) av[e] = col0 + e < d.n ? avbuf[e] : 0.f;
       }
-      if (row) row[j] = o[0][e];
+    }
+    if (live) {
+      const unsigned char *slot = pipe + (size_t)(st % kPipeStages) * slot_step + (size_t)threadIdx.x * RB;
+      reduce_plane<float, VW, GL>(
+          i, w, wz,
+          [&](int j, int k, float(&c)[VW]) {
+            const Raw *rp = reinterpret_cast<const Raw *>(slot + (j * 4 + k) * row_step);
+            if (WIDE) {
+              float lo[CT<ST>::VW], hi[CT<ST>::VW];
+              CT<ST>::decode(rp[0], lo);
+              CT<ST>::decode(rp[1], hi);
+#pragma unroll
+              for (int e = 0; e < CT<ST>::VW; e++) { c[e] = lo[e]; c[CT<ST>::VW + e] = hi[e]; }
+            } else {
+              CT<ST>::decode(rp[0], *reinterpret_cast<float(*)[CT<ST>::VW]>(&c[0]));
+            }
+          },
+          o);
+    }
+    if (i == 3) {
+      if (live) {
+        if (a.scale) {
+#pragma unroll
+          for (int e = 0; e < VW; e++) {
+            const float sc = a.scale[col0 + e];
+#pragma unroll
+            for (int q = 0; q < (GL ? 10 : 1); q++) o[q][e] *= sc;
+          }
+        }
+        float *row = d.row_out ? d.row_out[ssrc[pp]] : nullptr;
+#pragma unroll
+        for (int e = 0; e < VW; e++) {
+          acc[0] = fmaf(o[0][e], av[e], acc[0]);
+          if (GL) {
+            acc[1] = fmaf(o[1][e], av[e], acc[1]);
+            acc[2] = fmaf(o[2][e], av[e], acc[2]);
+            acc[3] = fmaf(o[3][e], av[e], acc[3]);
+            acc[4] = fmaf((o[4][e] + o[7][e]) + o[9][e], av[e], acc[4]);
+          }
+          if (row && col0 + e < d.n) row[col0 + e] = o[0][e];
+        }
+      }
+      zero_out<float, VW>(o);
+      if (g == G - 1) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
+          if ((threadIdx.x & 31) == 0) red[(pp * NW + (threadIdx.x >> 5)) * 5 + q] = acc[q];
+          acc[q] = 0.f;
+        }
+      }
     }
   }
-#pragma unroll
-  for (int q = 0; q < 5; q++)
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
-  const int warp = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0)
-#pragma unroll
-    for (int q = 0; q < 5; q++) red[warp][q] = acc[q];
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if ((int)threadIdx.x < pn) {
+    const int pp = threadIdx.x;
     float s[5];
 #pragma unroll
     for (int q = 0; q < 5; q++) {
-      s[q] = red[0][q];
+      s[q] = red[pp * NW * 5 + q];
 #pragma unroll
-      for (int r = 1; r < kDetThreads / 32; r++) s[q] += red[r][q];
+      for (int r = 1; r < NW; r++) s[q] += red[(pp * NW + r) * 5 + q];
     }
-    d.ratio[w] = s[0];
+    const int64_t wk = ssrc[pp];
+    d.ratio[wk] = s[0];
     if (GL) {
       const float inv = 1.0f / s[0];
       if (d.grad) {
-        d.grad[3 * (int64_t)w] = s[1] * inv;
-        d.grad[3 * (int64_t)w + 1] = s[2] * inv;
-        d.grad[3 * (int64_t)w + 2] = s[3] * inv;
+        d.grad[3 * wk] = s[1] * inv;
+        d.grad[3 * wk + 1] = s[2] * inv;
+        d.grad[3 * wk + 2] = s[3] * inv;
       }
-      if (d.lapl) d.lapl[w] = s[4] * inv;
+      if (d.lapl) d.lapl[wk] = s[4] * inv;
     }
   }
 }
@@ -157,7 +258,8 @@ __global__ void __launch_bounds__(256) k_det_update1_rows(const DetArgs d) {
 }
 
 // Pass 1, transposed layout (AinvT[c][j]): warp per row c, a dot product
-// with delta; the warp on row k also copies that row (column k of Ainv).
+// with delta (16-byte loads when the rows allow); the warp on row k also
+// copies that row (column k of Ainv).
 __global__ void __launch_bounds__(256) k_det_update1_trans(const DetArgs d) {
   const int w = blockIdx.y;
   const int c = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -166,10 +268,26 @@ __global__ void __launch_bounds__(256) k_det_update1_trans(const DetArgs d) {
   const float *u = d.urow[w];
   const float *ak = d.amat[w] + (int64_t)d.k * d.ld;
   float *x = d.work + (int64_t)w * 2 * d.n, *colk = x + d.n;
+  const bool copy = c == d.k;
   float acc = 0.f;
-  for (int j = lane; j < d.n; j += 32) {
+  int j0 = 0;
+  if (al16(ainvr) && al16(u) && al16(ak) && (!copy || al16(colk))) {
+    const int n4 = d.n >> 2;
+    for (int q = lane; q < n4; q += 32) {
+      const float4 v = reinterpret_cast<const float4 *>(ainvr)[q];
+      const float4 uu = reinterpret_cast<const float4 *>(u)[q];
+      const float4 aa = reinterpret_cast<const float4 *>(ak)[q];
+      if (copy) reinterpret_cast<float4 *>(colk)[q] = v;
+      acc = fmaf(v.x, uu.x - aa.x, acc);
+      acc = fmaf(v.y, uu.y - aa.y, acc);
+      acc = fmaf(v.z, uu.z - aa.z, acc);
+      acc = fmaf(v.w, uu.w - aa.w, acc);
+    }
+    j0 = n4 << 2;
+  }
+  for (int j = j0 + lane; j < d.n; j += 32) {
     const float v = ainvr[j];
-    if (c == d.k) colk[j] = v;
+    if (copy) colk[j] = v;
     acc = fmaf(v, u[j] - ak[j], acc);
   }
 #pragma unroll
@@ -177,26 +295,43 @@ __global__ void __launch_bounds__(256) k_det_update1_trans(const DetArgs d) {
   if (lane == 0) x[c] = acc;
 }
 
-// Pass 2: rank-1 correction of every entry and the new row of A.
-// Row r of the stored matrix: orbital j = r (reference layout) or electron
-// c = r (transposed).
+// Pass 2: rank-1 correction of every entry and the new row of A; warp per
+// stored row, 16-byte accesses when the row allows.  Entry (orbital j,
+// electron c) becomes Ainv + x[c] * (p * colk[j]) in both layouts (the
+// reference's kernel 2 expression, src/determinant_update.h:104-106).
 __global__ void __launch_bounds__(256) k_det_update2(const DetArgs d) {
   const int w = blockIdx.y;
-  const int r = blockIdx.x;
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (r >= d.n) return;
   const float *x = d.work + (int64_t)w * 2 * d.n, *colk = x + d.n;
   const float p = -1.0f / (1.0f + x[d.k]);
   float *m = const_cast<float *>(d.ainv[w]) + (int64_t)r * d.ld;
-  if (!d.trans) {
-    const float f = p * colk[r];
-    for (int c = threadIdx.x; c < d.n; c += blockDim.x) m[c] = fmaf(x[c], f, m[c]);
-  } else {
-    const float xr = x[r];
-    for (int j = threadIdx.x; j < d.n; j += blockDim.x) m[j] = fmaf(xr, p * colk[j], m[j]);
+  // reference layout: row r is orbital j = r, columns are electrons c;
+  // transposed: row r is electron c = r, columns are orbitals j
+  const float *vec = d.trans ? colk : x;
+  const float rs = d.trans ? x[r] : p * colk[r];
+  int i0 = 0;
+  if (al16(m) && al16(vec)) {
+    const int n4 = d.n >> 2;
+    for (int q = lane; q < n4; q += 32) {
+      float4 mv = reinterpret_cast<float4 *>(m)[q];
+      const float4 v = reinterpret_cast<const float4 *>(vec)[q];
+      if (d.trans) {
+        mv.x = fmaf(rs, p * v.x, mv.x); mv.y = fmaf(rs, p * v.y, mv.y);
+        mv.z = fmaf(rs, p * v.z, mv.z); mv.w = fmaf(rs, p * v.w, mv.w);
+      } else {
+        mv.x = fmaf(v.x, rs, mv.x); mv.y = fmaf(v.y, rs, mv.y);
+        mv.z = fmaf(v.z, rs, mv.z); mv.w = fmaf(v.w, rs, mv.w);
+      }
+      reinterpret_cast<float4 *>(m)[q] = mv;
+    }
+    i0 = n4 << 2;
   }
+  for (int i = i0 + lane; i < d.n; i += 32) m[i] = d.trans ? fmaf(rs, p * vec[i], m[i]) : fmaf(vec[i], rs, m[i]);
   if (r == d.k) {
     float *ak = d.amat[w] + (int64_t)d.k * d.ld;
     const float *u = d.urow[w];
-    for (int j = threadIdx.x; j < d.n; j += blockDim.x) ak[j] = u[j];
+    for (int j = lane; j < d.n; j += 32) ak[j] = u[j];
   }
 }
 
@@ -205,6 +340,16 @@ __global__ void __launch_bounds__(256) k_det_update2(const DetArgs d) {
 using namespace eg;
 
 namespace {
+
+int num_sms() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 152;
+  }
+  return n;
+}
 
 int check_det_opts(const einspline_gb300_det_opts *o, const char *fn) {
   if (!o) return fail(EINSPLINE_GB300_EINVAL, "%s: NULL options", fn);
@@ -216,10 +361,21 @@ int check_det_opts(const einspline_gb300_det_opts *o, const char *fn) {
   return 0;
 }
 
+template <int ST, bool GL>
+cudaError_t launch_ratio_k(const DetArgs &d, unsigned grid, cudaStream_t s) {
+  constexpr bool WIDE = ST != ST_F32;
+  constexpr int RB = WIDE ? 16 : (int)sizeof(typename CT<ST>::Raw);
+  const size_t sm = det_smem(d.e.pb, RB);
+  const void *f = (const void *)k_det_ratio<ST, GL, WIDE>;
+  cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_det_ratio<ST, GL, WIDE><<<grid, kDetThreads, sm, s>>>(d);
+  return cudaGetLastError();
+}
+
 template <int ST>
-void launch_ratio(const DetArgs &d, bool gl, int nw, cudaStream_t s) {
-  if (gl) k_det_ratio<ST, true><<<nw, kDetThreads, 0, s>>>(d);
-  else k_det_ratio<ST, false><<<nw, kDetThreads, 0, s>>>(d);
+cudaError_t launch_ratio(const DetArgs &d, bool gl, unsigned grid, cudaStream_t s) {
+  return gl ? launch_ratio_k<ST, true>(d, grid, s) : launch_ratio_k<ST, false>(d, grid, s);
 }
 
 }  // namespace
@@ -258,13 +414,24 @@ int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_de
   d.trans = o->ainv_trans;
   const bool gl = grad_d || lapl_d;
   cudaStream_t s = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+  // Two blocks fit on an SM (their copy pipelines take 96 KB each).  The
+  // walkers are spread evenly over at most one wave of such blocks, so each
+  // block runs one long pipeline over its walkers (no per-block fill and
+  // drain for every walker, no partial last wave); beyond 32 walkers per
+  // block the grid grows instead.
+  const int slots = 2 * num_sms();
+  int pb = (nwalkers + slots - 1) / slots;
+  pb = pb < 1 ? 1 : (pb > 32 ? 32 : pb);
+  d.e.pb = pb;
+  const unsigned grid = (unsigned)((nwalkers + pb - 1) / pb);
+  cudaError_t e;
   switch (t->storage) {
-    case ST_F32: launch_ratio<ST_F32>(d, gl, nwalkers, s); break;
-    case ST_F16: launch_ratio<ST_F16>(d, gl, nwalkers, s); break;
-    case ST_BF16: launch_ratio<ST_BF16>(d, gl, nwalkers, s); break;
-    default: launch_ratio<ST_I16>(d, gl, nwalkers, s); break;
+    case ST_F32: e = launch_ratio<ST_F32>(d, gl, grid, s); break;
+    case ST_F16: e = launch_ratio<ST_F16>(d, gl, grid, s); break;
+    case ST_BF16: e = launch_ratio<ST_BF16>(d, gl, grid, s); break;
+    default: e = launch_ratio<ST_I16>(d, gl, grid, s); break;
   }
-  EG_CUDA(cudaGetLastError());
+  EG_CUDA(e);
   count_launch();
   return 0;
 }
@@ -292,7 +459,7 @@ int einspline_gb300_det_update(const einspline_gb300_det_opts *o, int naccept, f
   if (!d.trans) k_det_update1_rows<<<dim3((d.n + 255) / 256, naccept), 256, 0, s>>>(d);
   else k_det_update1_trans<<<dim3((d.n + 7) / 8, naccept), 256, 0, s>>>(d);
   EG_CUDA(cudaGetLastError());
-  k_det_update2<<<dim3(d.n, naccept), 256, 0, s>>>(d);
+  k_det_update2<<<dim3((d.n + 7) / 8, naccept), 256, 0, s>>>(d);
   EG_CUDA(cudaGetLastError());
   count_launch(2);
   return 0;

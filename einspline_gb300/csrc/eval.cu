@@ -36,8 +36,6 @@ __device__ __forceinline__ void st_vec(double *p, const double (&v)[N]) {
 #pragma unroll
   for (int c = 0; c < N / 2; c++) __stcs(reinterpret_cast<double2 *>(p) + c, make_double2(v[2 * c], v[2 * c + 1]));
 }
-__device__ __forceinline__ bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
-
 // Index of Hessian entry m (row-major 3x3) among (xx, xy, xz, yy, yz, zz).
 __device__ __forceinline__ int h9to6(int m) {
   return (m == 0) ? 0 : (m == 1 || m == 3) ? 1 : (m == 2 || m == 6) ? 2 : (m == 4) ? 3 : (m == 5 || m == 7) ? 4 : 5;
@@ -186,14 +184,6 @@ __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col
   }
 }
 
-__host__ __device__ __forceinline__ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
-
-// Shared memory: pb * 36 weights, pb * 3 cell indices, pb source indices.
-__host__ __device__ __forceinline__ size_t smem_w_bytes(int pb, int accb) { return align_up((size_t)pb * 36 * accb, 16); }
-__host__ __device__ __forceinline__ size_t smem_total(int pb, int accb) {
-  return smem_w_bytes(pb, accb) + align_up((size_t)pb * 3 * 4, 8) + (size_t)pb * 8;
-}
-
 template <int ST, bool VGH>
 __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
   using A = typename CT<ST>::A;
@@ -252,42 +242,6 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
     epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
   }
 }
-
-// Points' cells, weights and sources into shared memory (both kernels).
-template <typename A>
-__device__ __forceinline__ int eval_prologue(const EvalArgs &a, unsigned char *smem, int64_t p0, int tid, int nthr) {
-  A *sw = reinterpret_cast<A *>(smem);
-  int *sidx = reinterpret_cast<int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
-  int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
-  const int pn = (int)min((int64_t)a.pb, a.npts - p0);
-  for (int q = tid; q < pn * 3; q += nthr) {
-    const int pp = q / 3, ax = q - 3 * pp;
-    const int64_t src = a.perm ? (int64_t)a.perm[p0 + pp] : p0 + pp;
-    double xd;
-    if (!a.pos) xd = a.inl[ax];
-    else if (a.pos_f64) xd = reinterpret_cast<const double *>(a.pos)[3 * src + ax];
-    else xd = (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
-    int idx;
-    A t;
-    cell(a, ax, xd, idx, t);
-    bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
-    sidx[pp * 3 + ax] = idx;
-    if (ax == 0) ssrc[pp] = src;
-  }
-  return pn;
-}
-
-template <int RB>
-__device__ __forceinline__ void cp_async(unsigned dst, const char *src) {
-  if (RB == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-  else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-constexpr int kPipeStages = 3;
-__host__ __device__ __forceinline__ size_t pipe_bytes(int nthr, int rb) { return (size_t)kPipeStages * 16 * nthr * rb; }
 
 // Pipelined variant: a stage is one x-plane (16 stencil rows) of one point.
 // Each thread copies its own columns of the rows of stage s+2 into shared

@@ -67,6 +67,9 @@ __device__ __forceinline__ void load_row(const char *p, typename CT<ST>::A (&v)[
 }
 
 
+// 16-byte alignment of a device address.
+__device__ __forceinline__ bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
 __device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
 
@@ -235,5 +238,53 @@ __device__ __forceinline__ void contract(const char *base, int64_t xsb, int64_t 
                              o);
   }
 }
+
+__host__ __device__ __forceinline__ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Shared memory: pb * 36 weights, pb * 3 cell indices, pb source indices.
+__host__ __device__ __forceinline__ size_t smem_w_bytes(int pb, int accb) { return align_up((size_t)pb * 36 * accb, 16); }
+__host__ __device__ __forceinline__ size_t smem_total(int pb, int accb) {
+  return smem_w_bytes(pb, accb) + align_up((size_t)pb * 3 * 4, 8) + (size_t)pb * 8;
+}
+
+// Points' cells, weights and sources into shared memory (evaluation and determinant kernels).
+template <typename A>
+__device__ __forceinline__ int eval_prologue(const EvalArgs &a, unsigned char *smem, int64_t p0, int tid, int nthr) {
+  A *sw = reinterpret_cast<A *>(smem);
+  int *sidx = reinterpret_cast<int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
+  int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
+  const int pn = (int)min((int64_t)a.pb, a.npts - p0);
+  for (int q = tid; q < pn * 3; q += nthr) {
+    const int pp = q / 3, ax = q - 3 * pp;
+    const int64_t src = a.perm ? (int64_t)a.perm[p0 + pp] : p0 + pp;
+    double xd;
+    if (!a.pos) xd = a.inl[ax];
+    else if (a.pos_f64) xd = reinterpret_cast<const double *>(a.pos)[3 * src + ax];
+    else xd = (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
+    int idx;
+    A t;
+    cell(a, ax, xd, idx, t);
+    bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
+    sidx[pp * 3 + ax] = idx;
+    if (ax == 0) ssrc[pp] = src;
+  }
+  return pn;
+}
+
+// Asynchronous global-to-shared copy of RB = 4, 8 or 16 bytes (both
+// addresses RB-aligned); 16-byte copies bypass L1.
+template <int RB>
+__device__ __forceinline__ void cp_async(unsigned dst, const char *src) {
+  static_assert(RB == 4 || RB == 8 || RB == 16, "cp.async copies 4, 8 or 16 bytes");
+  if constexpr (RB == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  else if constexpr (RB == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int kPipeStages = 3;
+__host__ __device__ __forceinline__ size_t pipe_bytes(int nthr, int rb) { return (size_t)kPipeStages * 16 * nthr * rb; }
 
 }  // namespace eg

@@ -7,6 +7,7 @@ Everything it touches is a few GB, larger than L2, so DRAM counters of one
 launch mean what they mean in the benchmark.
 
     python -m einspline_gb300.profile_case --storage f16 --launches 3
+    python -m einspline_gb300.profile_case --storage f16 --det 2048  # fused determinant ratio
 """
 from __future__ import annotations
 
@@ -28,6 +29,9 @@ def main():
     ap.add_argument("--sort", type=int, default=0)
     ap.add_argument("--mode", type=int, default=-1, help="load mode: 0 direct, 1 L2 prefetch, 2 smem pipeline")
     ap.add_argument("--sweep", type=int, default=0, help="time every tile shape in every load mode")
+    ap.add_argument("--det", type=int, default=0,
+                    help="W > 0: time the fused determinant ratio (value, gradient, Laplacian; transposed "
+                         "inverses) of W walkers over all splines instead")
     args = ap.parse_args()
 
     import torch
@@ -43,6 +47,29 @@ def main():
         T.set_device(f, buf[:n])
     T.flush()
     del buf
+    if args.det:
+        # The ratio reads only row k of each transposed inverse: with k = 0 a
+        # [W][1][N] buffer (row 0 of every walker's N x N matrix) is all the
+        # kernel touches, so the capture holds megabytes, not W * N * N floats.
+        W, N = args.det, args.splines
+        Ai = torch.empty((W, 1, N), dtype=torch.float32, device="cuda")
+        api.fill_uniform(Ai, 92, -1.0, 1.0)
+        D = api.Determinants(Ai, Ai, N, trans=1)
+        pos = torch.from_numpy(synth.points_uniform(779, W).astype(np.float32)).cuda()
+        D.ratio(T, pos, 0, grad_lapl=True)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(args.launches):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            D.ratio(T, pos, 0, grad_lapl=True)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        bpe = 64 * (4 if st == api.STORE_F32 else 2) + 4
+        print(json.dumps({"storage": args.storage, "walkers": W, "orbitals": N, "ms": times, "bytes_per_eval": bpe,
+                          "GBps": [W * N * bpe / (t * 1e-3) / 1e9 for t in times]}))
+        return
     if args.tile:
         T.set_tile(*args.tile)
     T.set_load_mode(args.mode)

@@ -11,24 +11,59 @@ from helpers import build_pair
 
 P = 0
 GRIDS = [(0.0, 1.0, 12), (0.0, 1.0, 11), (0.0, 1.0, 13)]
+SMALL = [(0.0, 1.0, 7), (0.0, 1.0, 8), (0.0, 1.0, 6)]
 NSPL, NELEC, LD = 40, 37, 40
 
 
-def _population(torch, orc, G, T, W, seed, trans):
+def _population(torch, orc, G, T, W, seed, trans, nelec=NELEC, ld=LD, distinct=None):
     """W walkers: electrons at random positions, A[e][j] = phi_j(r_e) from the
-    oracle (GPU cell rule), Ainv = inv(A); float32 on the device."""
+    oracle (GPU cell rule), Ainv = inv(A); float32 on the device.  With
+    distinct=m only m different matrices are made and repeated."""
     rng = np.random.default_rng(seed)
-    A = np.zeros((W, LD, LD), np.float32)
-    Ai = np.zeros((W, LD, LD), np.float32)
-    for w in range(W):
-        R = rng.random((NELEC, 3))
-        v = T.eval(R, vgh=False, sem=1)[0][:, :NELEC].astype(np.float64)
-        A[w, :NELEC, :NELEC] = v
+    A = np.zeros((W, ld, ld), np.float32)
+    Ai = np.zeros((W, ld, ld), np.float32)
+    m = W if distinct is None else distinct
+    for w in range(m):
+        R = rng.random((nelec, 3))
+        v = T.eval(R, vgh=False, sem=1)[0][:, :nelec].astype(np.float64)
+        A[w, :nelec, :nelec] = v
         inv = np.linalg.inv(v)
-        Ai[w, :NELEC, :NELEC] = inv.T if trans else inv
+        Ai[w, :nelec, :nelec] = inv.T if trans else inv
+    for w in range(m, W):
+        A[w], Ai[w] = A[w % m], Ai[w % m]
     dev = "cuda"
-    D = api.Determinants(torch.from_numpy(A).to(dev), torch.from_numpy(Ai).to(dev), NELEC, trans=trans)
+    D = api.Determinants(torch.from_numpy(A).to(dev), torch.from_numpy(Ai).to(dev), nelec, trans=trans)
     return D, A, Ai
+
+
+def _check_ratio(orc, torch, G, D, Ai, pos, k, trans, nelec):
+    """Ratios of the fused kernel against float64 sums of the flat
+    evaluation's per-orbital outputs, the value row bit for bit."""
+    W, ld = Ai.shape[0], Ai.shape[1]
+    rows = torch.zeros(W, ld, dtype=torch.float32, device="cuda")
+    r, g, lap = D.ratio(G, pos, k, grad_lapl=True, rows=rows)
+    r0, g0, l0 = D.ratio(G, pos, k, grad_lapl=False)
+    r2, g2, l2 = D.ratio(G, pos, k, grad_lapl=True)
+    torch.cuda.synchronize()
+    assert torch.equal(r, r2) and torch.equal(g, g2) and torch.equal(lap, l2)
+    assert g0 is None and l0 is None
+    v, gr, h = G.eval(pos, vgh=True, rule=1, layout=1)
+    assert torch.equal(rows[:, :nelec], v[:, :nelec])
+    assert torch.count_nonzero(rows[:, nelec:]) == 0
+    Astd = _ainv_std(Ai, trans)[:, :nelec, :nelec]
+    vv, gg, hh = (x.cpu().numpy()[:, :nelec] for x in (v, gr, h))
+    ref = orc.det_ratio(vv, gg, hh, Astd, k)
+    sr, sg, sl = orc.det_ratio_bound(vv, gg, hh, Astd, k)
+    R = r.cpu().numpy().astype(np.float64)
+    eps = 1e-5
+    assert np.all(np.abs(R - ref[0]) <= eps * sr)
+    assert np.all(np.abs(r0.cpu().numpy() - ref[0]) <= eps * sr)
+    Rr = np.abs(ref[0])
+    gb = eps * (sg / Rr[:, None] + np.abs(ref[1]) * (sr / Rr)[:, None])
+    assert np.all(np.abs(g.cpu().numpy() - ref[1]) <= gb)
+    lb = eps * (sl / Rr + np.abs(ref[2]) * sr / Rr)
+    assert np.all(np.abs(lap.cpu().numpy() - ref[2]) <= lb)
+    return R, Astd
 
 
 def _ainv_std(Ai, trans):
@@ -45,37 +80,39 @@ def test_det_ratio(orc, trans, storage):
     W, k = 9, 5
     D, A, Ai = _population(torch, orc, G, T, W, 302, trans)
     pos = torch.from_numpy(synth.points_uniform(303, W, [0.0] * 3, [1.0] * 3).astype(np.float32)).cuda()
-    rows = torch.zeros(W, LD, dtype=torch.float32, device="cuda")
-    r, g, lap = D.ratio(G, pos, k, grad_lapl=True, rows=rows)
-    r0, g0, l0 = D.ratio(G, pos, k, grad_lapl=False)
-    r2, g2, l2 = D.ratio(G, pos, k, grad_lapl=True)
-    torch.cuda.synchronize()
-    # deterministic, and the value-only kernel gives the same ratio
-    assert torch.equal(r, r2) and torch.equal(g, g2) and torch.equal(lap, l2)
-    assert g0 is None and l0 is None
-    # the row equals the flat evaluation's values bit for bit
-    v, gr, h = G.eval(pos, vgh=True, rule=1, layout=1)
-    assert torch.equal(rows[:, :NELEC], v[:, :NELEC])
-    assert torch.count_nonzero(rows[:, NELEC:]) == 0
-    # ratios against float64 sums of the per-orbital outputs
-    Astd = _ainv_std(Ai, trans)
-    vv, gg, hh = (x.cpu().numpy()[:, :NELEC] for x in (v, gr, h))
-    ref = orc.det_ratio(vv, gg, hh, Astd[:, :NELEC, :NELEC], k)
-    sr, sg, sl = orc.det_ratio_bound(vv, gg, hh, Astd[:, :NELEC, :NELEC], k)
-    R = r.cpu().numpy().astype(np.float64)
-    eps = 1e-5
-    assert np.all(np.abs(R - ref[0]) <= eps * sr)
-    assert np.all(np.abs(r0.cpu().numpy() - ref[0]) <= eps * sr)
-    Rr = np.abs(ref[0])
-    gb = eps * (sg / Rr[:, None] + np.abs(ref[1]) * (sr / Rr)[:, None])
-    assert np.all(np.abs(g.cpu().numpy() - ref[1]) <= gb)
-    lb = eps * (sl / Rr + np.abs(ref[2]) * sr / Rr)
-    assert np.all(np.abs(lap.cpu().numpy() - ref[2]) <= lb)
+    R, Astd = _check_ratio(orc, torch, G, D, Ai, pos, k, trans, NELEC)
     if storage == api.STORE_F32:
         # and against the oracle's own evaluation of the same table
         ov, og, oh = (x[:, :NELEC] for x in T.eval(pos.cpu().numpy().astype(np.float64), vgh=True, sem=1))
-        oref = orc.det_ratio(ov, og, oh, Astd[:, :NELEC, :NELEC], k)
-        assert np.all(np.abs(R - oref[0]) <= 4 * eps * sr)
+        oref = orc.det_ratio(ov, og, oh, Astd, k)
+        sr = orc.det_ratio_bound(ov, og, oh, Astd, k)[0]
+        assert np.all(np.abs(R - oref[0]) <= 4e-5 * sr)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage,nelec", [(api.STORE_F32, 600), (api.STORE_F16, 1100)])
+def test_det_ratio_column_groups(orc, storage, nelec):
+    """More orbitals than one block's column group (512 FP32 / 1024 16-bit
+    columns): the per-walker sums run over several groups."""
+    torch = pytest.importorskip("torch")
+    nspl, ld = nelec + 24, nelec + 4
+    G, T, _ = build_pair(orc, "s", SMALL, [(P, P)] * 3, nspl, seed=341, storage=storage)
+    W, k = 3, nelec - 2
+    D, A, Ai = _population(torch, orc, G, T, W, 342, 1, nelec=nelec, ld=ld)
+    pos = torch.from_numpy(synth.points_uniform(343, W, [0.0] * 3, [1.0] * 3).astype(np.float32)).cuda()
+    _check_ratio(orc, torch, G, D, Ai, pos, k, 1, nelec)
+
+
+@pytest.mark.gpu
+def test_det_ratio_many_walkers(orc):
+    """Enough walkers that a block takes several (the launch packs walkers
+    per block once the grid has four waves of two blocks per SM)."""
+    torch = pytest.importorskip("torch")
+    G, T, _ = build_pair(orc, "s", GRIDS, [(P, P)] * 3, NSPL, seed=351, storage=api.STORE_F16)
+    W, k = 5000, 11
+    D, A, Ai = _population(torch, orc, G, T, W, 352, 0, distinct=16)
+    pos = torch.from_numpy(synth.points_uniform(353, W, [0.0] * 3, [1.0] * 3).astype(np.float32)).cuda()
+    _check_ratio(orc, torch, G, D, Ai, pos, k, 0, NELEC)
 
 
 @pytest.mark.gpu
