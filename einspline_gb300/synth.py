@@ -76,8 +76,10 @@ def grid_data_planewaves(seed: int, M: tuple, num_splines: int, waves: int = 8, 
 
 
 def points_uniform(seed: int, npts: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0)) -> np.ndarray:
-    """npts points uniform in the box [lo, hi), shape (npts, 3) float64."""
-    u = uniform(seed, 3 * npts, 0.0, 1.0).reshape(npts, 3)
+    """npts points uniform in the box [lo, hi), shape (npts, len(lo)) float64
+    (3 coordinates by default; 1 or 2 for the 1D/2D multi-splines)."""
+    dims = len(lo)
+    u = uniform(seed, dims * npts, 0.0, 1.0).reshape(npts, dims)
     lo = np.asarray(lo, np.float64)
     hi = np.asarray(hi, np.float64)
     p = lo + (hi - lo) * u

@@ -237,6 +237,28 @@ void orc_set_3d_column_d(const orc_desc *d, int ncomp, int spline, double *table
   (void)Nz;
 }
 
+/* The same for 1D and 2D multi-splines (dims = 1 or 2: axes beyond dims
+ * have num = ncoef = 1): sweeps along x, then y
+ * (src/multi_bspline_create.c:822-828 and :903-940 for d, :1138-1145 and
+ * :1257-1300 for z). */
+void orc_set_column_d(const orc_desc *d, int dims, int ncomp, int spline, double *table, const double *data)
+{
+  if (dims == 3) { orc_set_3d_column_d(d, ncomp, spline, table, data); return; }
+  const orc_axis *X = &d->ax[0], *Y = &d->ax[1];
+  const int My = dims == 2 ? Y->num : 1;
+  const int Nx = X->ncoef;
+  const int64_t xs = ncomp * d->xs, ys = ncomp * d->ys;
+  for (int p = 0; p < ncomp; p++) {
+    double *col = table + (int64_t)ncomp * spline + p;
+    const double *dat = data + p;
+    for (int iy = 0; iy < My; iy++)
+      orc_find_coefs_1d_d(X, p, dat + (int64_t)ncomp * iy, (int64_t)ncomp * My, col + iy*ys, xs);
+    if (dims == 2)
+      for (int ix = 0; ix < Nx; ix++)
+        orc_find_coefs_1d_d(Y, p, col + ix*xs, ys, col + ix*xs, ys);
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* Evaluation.                                                         */
 /* ------------------------------------------------------------------ */
@@ -535,6 +557,118 @@ void orc_eval_z_vghgh(const orc_desc *d, const double *coefs, double x, double y
 {
   enum { NC = 2 };
   ORC_VGHGH_BODY(double, cell_d, basis_d)
+}
+
+/* 1D and 2D multi-splines at one point, CPU-entry cell rule, the CPU API's
+ * layouts (src/multi_bspline_eval_std_s_impl.h:38-181 for 1D, :183-480 for
+ * 2D; _d, _c, _z impl files alike).  form: 0 value, 1 vg, 2 vgl, 3 vgh.
+ *   1D: vals[N], grads[N], lh[N] = second derivative (vgl and vgh alike: the
+ *       reference's 1D vgh calls vgl);
+ *   2D: vals[N], grads[N][2], lapl[N] (vgl: (xx + yy)), hess[N][2][2] (vgh).
+ * Products and sums in the reference's order: ab = a_i * b_j formed once
+ * per (i, j), accumulated over i then j, scaled by delta_inv afterwards.
+ * l2 is scratch of 2*N entries for the 2D vgl (the reference's lapl2). */
+#define ORC_LD_BODY(REAL, CELL, BASIS)                                           \
+  const int N = d->num_splines;                                                  \
+  int ix, iy = 0; REAL tx, ty = 0;                                               \
+  CELL(&d->ax[0], 0, x, &ix, &tx);                                               \
+  REAL wa[3][4], wb[3][4];                                                       \
+  BASIS(tx, wa);                                                                 \
+  if (dims == 2) { CELL(&d->ax[1], 0, y, &iy, &ty); BASIS(ty, wb); }            \
+  const int64_t xs = NC * d->xs, ys = NC * d->ys;                                \
+  const int ng = dims;                                                           \
+  for (int n = 0; n < NC * N; n++) vals[n] = 0;                                  \
+  if (form >= 1) for (int n = 0; n < ng * NC * N; n++) grads[n] = 0;            \
+  if (dims == 1 && form >= 2) for (int n = 0; n < NC * N; n++) lh[n] = 0;       \
+  if (dims == 2 && form == 2) for (int n = 0; n < 2 * NC * N; n++) l2[n] = 0;   \
+  if (dims == 2 && form == 3) for (int n = 0; n < 4 * NC * N; n++) lh[n] = 0;   \
+  if (dims == 1) {                                                               \
+    for (int i = 0; i < 4; i++) {                                                \
+      const REAL *cf = coefs + (ix+i)*xs;                                        \
+      for (int n = 0; n < NC * N; n++) {                                         \
+        vals[n] += wa[0][i] * cf[n];                                             \
+        if (form >= 1) grads[n] += wa[1][i] * cf[n];                             \
+        if (form >= 2) lh[n] += wa[2][i] * cf[n];                                \
+      }                                                                          \
+    }                                                                            \
+    REAL dx = (REAL)d->ax[0].delta_inv;                                          \
+    for (int n = 0; n < NC * N; n++) {                                           \
+      if (form >= 1) grads[n] *= dx;                                             \
+      if (form >= 2) lh[n] *= dx*dx;                                             \
+    }                                                                            \
+  } else {                                                                       \
+    for (int i = 0; i < 4; i++)                                                  \
+      for (int j = 0; j < 4; j++) {                                              \
+        REAL ab = wa[0][i]*wb[0][j];                                             \
+        REAL dab0 = wa[1][i]*wb[0][j], dab1 = wa[0][i]*wb[1][j];                 \
+        REAL e0 = 0, e1 = 0, e2 = 0;                                             \
+        if (form == 2) { e0 = wa[2][i]*wb[0][j]; e1 = wa[0][i]*wb[2][j]; }       \
+        if (form == 3) { e0 = wa[2][i]*wb[0][j]; e1 = wa[1][i]*wb[1][j];         \
+                         e2 = wa[0][i]*wb[2][j]; }                               \
+        const REAL *cf = coefs + (ix+i)*xs + (iy+j)*ys;                          \
+        for (int n = 0; n < N; n++)                                              \
+          for (int p = 0; p < NC; p++) {                                         \
+            REAL c = cf[NC*n + p];                                               \
+            vals[NC*n + p] += ab * c;                                            \
+            if (form >= 1) {                                                     \
+              grads[NC*(2*n+0) + p] += dab0 * c;                                 \
+              grads[NC*(2*n+1) + p] += dab1 * c;                                 \
+            }                                                                    \
+            if (form == 2) {                                                     \
+              l2[NC*(2*n+0) + p] += e0 * c;                                      \
+              l2[NC*(2*n+1) + p] += e1 * c;                                      \
+            }                                                                    \
+            if (form == 3) {                                                     \
+              lh[NC*(4*n+0) + p] += e0 * c;                                      \
+              lh[NC*(4*n+1) + p] += e1 * c;                                      \
+              lh[NC*(4*n+3) + p] += e2 * c;                                      \
+            }                                                                    \
+          }                                                                      \
+      }                                                                          \
+    REAL dx = (REAL)d->ax[0].delta_inv, dy = (REAL)d->ax[1].delta_inv;           \
+    for (int n = 0; n < N; n++)                                                  \
+      for (int p = 0; p < NC; p++) {                                             \
+        if (form >= 1) {                                                         \
+          grads[NC*(2*n+0) + p] *= dx;                                           \
+          grads[NC*(2*n+1) + p] *= dy;                                           \
+        }                                                                        \
+        if (form == 2) {                                                         \
+          l2[NC*(2*n+0) + p] *= dx*dx;                                           \
+          l2[NC*(2*n+1) + p] *= dy*dy;                                           \
+          lh[NC*n + p] = l2[NC*(2*n+0) + p] + l2[NC*(2*n+1) + p];                \
+        }                                                                        \
+        if (form == 3) {                                                         \
+          lh[NC*(4*n+0) + p] *= dx*dx;                                           \
+          lh[NC*(4*n+1) + p] *= dx*dy;                                           \
+          lh[NC*(4*n+3) + p] *= dy*dy;                                           \
+          lh[NC*(4*n+2) + p] = lh[NC*(4*n+1) + p];                               \
+        }                                                                        \
+      }                                                                          \
+  }
+
+void orc_eval_ld_s(const orc_desc *d, int dims, int form, const float *coefs, double x, double y,
+                   float *vals, float *grads, float *lh, float *l2)
+{
+  enum { NC = 1 };
+  ORC_LD_BODY(float, cell_f, basis_f)
+}
+void orc_eval_ld_d(const orc_desc *d, int dims, int form, const double *coefs, double x, double y,
+                   double *vals, double *grads, double *lh, double *l2)
+{
+  enum { NC = 1 };
+  ORC_LD_BODY(double, cell_d, basis_d)
+}
+void orc_eval_ld_c(const orc_desc *d, int dims, int form, const float *coefs, double x, double y,
+                   float *vals, float *grads, float *lh, float *l2)
+{
+  enum { NC = 2 };
+  ORC_LD_BODY(float, cell_f, basis_f)
+}
+void orc_eval_ld_z(const orc_desc *d, int dims, int form, const double *coefs, double x, double y,
+                   double *vals, double *grads, double *lh, double *l2)
+{
+  enum { NC = 2 };
+  ORC_LD_BODY(double, cell_d, basis_d)
 }
 
 /* Many points, OpenMP over points as the reference's timing driver does

@@ -57,6 +57,10 @@ def lib(fast: bool = False) -> C.CDLL:
         L.orc_find_coefs_1d_d.argtypes = [C.POINTER(OrcAxis), C.c_int, C.c_void_p, C.c_int64,
                                           C.c_void_p, C.c_int64]
         L.orc_set_3d_column_d.argtypes = [C.POINTER(OrcDesc), C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        L.orc_set_column_d.argtypes = [C.POINTER(OrcDesc), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        for t in "sdcz":
+            getattr(L, f"orc_eval_ld_{t}").argtypes = [C.POINTER(OrcDesc), C.c_int, C.c_int, C.c_void_p, C.c_double,
+                                                      C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         for t in "sdcz":
             f = getattr(L, "orc_eval_" + t)
             f.argtypes = [C.POINTER(OrcDesc), C.c_int, C.c_int, C.c_void_p, C.c_double, C.c_double,
@@ -83,25 +87,31 @@ class Table:
     2 for re/im).  ``kind`` is one of 's','d','c','z'."""
 
     def __init__(self, kind, grids, bcs, num_splines):
-        # grids: 3 x (start, end, num); bcs: 3 x (lcode, rcode, lval_r, lval_i, rval_r, rval_i)
+        # grids: dims x (start, end, num); bcs: dims x (lcode, rcode, lval_r, lval_i, rval_r, rval_i),
+        # dims = 1, 2 or 3 (the 1D/2D/3D multi-splines)
         self.kind = kind
+        self.dims = len(grids)
         self.ncomp = 2 if kind in "cz" else 1
         self.dtype = np.float32 if kind in "sc" else np.float64
         self.desc = OrcDesc()
         L = lib()
         shape = []
-        for a in range(3):
+        for a in range(self.dims):
             st, en, num = grids[a]
             lc, rc, *vals = bcs[a]
             vals = list(vals) + [0.0] * (4 - len(vals))
             n = L.orc_axis_init(C.byref(self.desc.ax[a]), st, en, num, lc, rc, *vals)
             shape.append(n)
+        for a in range(self.dims, 3):        # absent axes: one point, one coefficient
+            self.desc.ax[a].num = 1
+            self.desc.ax[a].ncoef = 1
+        ext = list(shape) + [1] * (3 - self.dims)
         self.desc.num_splines = num_splines
         self.N = num_splines
         self.shape = tuple(shape)
         self.desc.zs = num_splines
-        self.desc.ys = shape[2] * num_splines
-        self.desc.xs = shape[1] * shape[2] * num_splines
+        self.desc.ys = ext[2] * num_splines
+        self.desc.xs = ext[1] * ext[2] * num_splines
         full = tuple(shape) + (num_splines,) + ((2,) if self.ncomp == 2 else ())
         # FP64 solve target; for s/c the table is this rounded to float32.
         self.coefs64 = np.zeros(full, dtype=np.float64)
@@ -115,7 +125,7 @@ class Table:
         """FP64 solve of one spline column (set_multi_UBspline_3d_d/z); data
         has shape (Mx,My,Mz) real or (Mx,My,Mz,2) / complex."""
         d = np.ascontiguousarray(_as_pairs(data, self.ncomp), dtype=np.float64)
-        lib().orc_set_3d_column_d(C.byref(self.desc), self.ncomp, i, ptr(self.coefs64), ptr(d))
+        lib().orc_set_column_d(C.byref(self.desc), self.dims, self.ncomp, i, ptr(self.coefs64), ptr(d))
         self._coefs = None
 
     @property
@@ -124,6 +134,18 @@ class Table:
         if self._coefs is None:
             self._coefs = np.ascontiguousarray(self.coefs64.astype(self.dtype))
         return self._coefs
+
+    def eval_ld(self, pos, form: int = 3, coefs: np.ndarray = None):
+        """1D/2D tables: eval_multi_UBspline_{1,2}d_* at each position (CPU
+        rule).  form 0 value, 1 vg, 2 vgl, 3 vgh.  Returns vals [P][N],
+        grads [P][N] (1D) or [P][N][2] (2D), and lh: the second derivative
+        [P][N] (1D vgl/vgh), the laplacian [P][N] (2D vgl) or the Hessian
+        [P][N][2][2] (2D vgh); complex types add a trailing axis of 2."""
+        assert self.dims in (1, 2)
+        cf = self.coefs if coefs is None else np.ascontiguousarray(coefs)
+        return _eval_ld(lambda v, g, lh, l2, x, y: getattr(lib(), f"orc_eval_ld_{self.kind}")(
+            C.byref(self.desc), self.dims, form, ptr(cf), x, y, ptr(v), ptr(g), ptr(lh), ptr(l2)),
+            self.dims, form, pos, self.dtype, self.N, self.ncomp)
 
     def eval_vghgh(self, pos: np.ndarray, coefs: np.ndarray = None):
         """Value, gradient, Hessian and third derivatives [P][N][3][3][3]
@@ -163,6 +185,27 @@ def _vghgh(fn, obj, pos, dtype, N, ncomp, coefs):
     for p in range(P):
         fn(obj, coefs, *[float(c) for c in pos[p]], v[p], g[p], h[p], gh[p])
     return v, g, h, gh
+
+
+def _eval_ld(fn, dims, form, pos, dtype, N, ncomp):
+    pos = np.asarray(pos, dtype=np.float64).reshape(-1, dims)
+    P = pos.shape[0]
+    ext = (2,) if ncomp == 2 else ()
+    v = np.zeros((P, N) + ext, dtype)
+    g = np.zeros((P, N) + ((dims,) if dims == 2 else ()) + ext, dtype)
+    if dims == 1:
+        lh = np.zeros((P, N) + ext, dtype)
+    else:
+        lh = np.zeros((P, N) + ((2, 2) if form == 3 else ()) + ext, dtype)
+    # one spare entry per buffer: the reference's 2D vg clears grads[2N]
+    gbuf = np.zeros(g[0].size + ncomp, dtype)
+    l2 = np.zeros(2 * N * ncomp + ncomp, dtype)
+    for p in range(P):
+        y = float(pos[p, 1]) if dims == 2 else 0.0
+        fn(v[p], gbuf, lh[p], l2, float(pos[p, 0]), y)
+        g[p] = gbuf[:g[0].size].reshape(g[0].shape)
+    out = [v, g if form >= 1 else None, lh if form >= 2 else None]
+    return out
 
 
 def _as_pairs(data, ncomp):
@@ -212,6 +255,20 @@ REF_BC = {"s": RefBC_s, "d": RefBC_d, "c": RefBC_c, "z": RefBC_z}
 REF_STRUCT = {k: _ref_struct(v) for k, v in REF_BC.items()}
 
 
+def _ref_struct_ld(bc_t, dims):
+    """multi_UBspline_{1,2}d_* (src/multi_bspline_structs.h:28-51 and alike);
+    the 2D complex structs' trailing lapl2 pointer is not read here."""
+    ax = "xy"[:dims]
+    fields = [("spcode", C.c_int), ("tcode", C.c_int), ("coefs", C.c_void_p)]
+    fields += [(f"{a}_stride", C.c_ssize_t) for a in ax] + [(f"{a}_grid", RefUgrid) for a in ax]
+    fields += [(f"{a}BC", bc_t) for a in ax] + [("num_splines", C.c_int)]
+    return type(f"RefMulti{dims}D", (C.Structure,), {"_fields_": fields})
+
+
+REF_STRUCT_LD = {(k, d): _ref_struct_ld(v, d) for k, v in REF_BC.items() for d in (1, 2)}
+LD_SUFFIX = ("", "_vg", "_vgl", "_vgh")
+
+
 def ref_available() -> bool:
     return os.path.exists(REF_LIB)
 
@@ -236,8 +293,75 @@ def ref_lib() -> C.CDLL:
                 C.POINTER(S), C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
             getattr(_ref, f"eval_multi_UBspline_3d_{t}_vghgh").argtypes = [
                 C.POINTER(S), C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        for t in "sdcz":
+            for dims in (1, 2):
+                S = REF_STRUCT_LD[(t, dims)]
+                f = getattr(_ref, f"create_multi_UBspline_{dims}d_{t}")
+                f.argtypes = [RefUgrid] * dims + [REF_BC[t]] * dims + [C.c_int]
+                f.restype = C.POINTER(S)
+                getattr(_ref, f"set_multi_UBspline_{dims}d_{t}").argtypes = [C.POINTER(S), C.c_int, C.c_void_p]
+                for form, suf in enumerate(LD_SUFFIX):
+                    getattr(_ref, f"eval_multi_UBspline_{dims}d_{t}{suf}").argtypes = (
+                        [C.POINTER(S)] + [C.c_double] * dims + [C.c_void_p] * (1 + min(form, 2)))
         _ref.destroy_Bspline.argtypes = [C.c_void_p]
     return _ref
+
+
+class RefSplineLD:
+    """A 1D or 2D multi-spline built by the reference's create/set."""
+
+    def __init__(self, kind, grids, bcs, num_splines):
+        L = ref_lib()
+        self.kind, self.N, self.dims = kind, num_splines, len(grids)
+        self.ncomp = 2 if kind in "cz" else 1
+        self.dtype = np.float32 if kind in "sc" else np.float64
+        ug = [RefUgrid(g[0], g[1], g[2], 0.0, 0.0) for g in grids]
+        BC = REF_BC[kind]
+        bcs_c = []
+        for b in bcs:
+            lc, rc, *v = b
+            v = list(v) + [0.0] * (4 - len(v))
+            bcs_c.append(BC(lc, rc, v[0], v[2]) if kind in "sd" else BC(lc, rc, v[0], v[1], v[2], v[3]))
+        self.p = getattr(L, f"create_multi_UBspline_{self.dims}d_{kind}")(*ug, *bcs_c, num_splines)
+        s = self.p.contents
+        self.shape = tuple(RefSpline._n(g, b) for g, b in zip(grids, bcs))
+        self.inner = s.y_stride if self.dims == 2 else s.x_stride
+
+    def set_spline(self, i, data):
+        d = np.ascontiguousarray(_as_pairs(data, self.ncomp), dtype=self.dtype)
+        getattr(ref_lib(), f"set_multi_UBspline_{self.dims}d_{self.kind}")(self.p, i, ptr(d))
+
+    def _view(self):
+        s = self.p.contents
+        n = self.shape[0] * s.x_stride * self.ncomp
+        buf = (C.c_float if self.dtype == np.float32 else C.c_double) * n
+        arr = np.frombuffer(buf.from_address(s.coefs), dtype=self.dtype)
+        return arr.reshape(self.shape + (self.inner,) + ((2,) if self.ncomp == 2 else ()))
+
+    def table(self) -> np.ndarray:
+        return self._view()[..., :self.N, :].copy() if self.ncomp == 2 else self._view()[..., :self.N].copy()
+
+    def load_table(self, coefs: np.ndarray) -> None:
+        v = self._view()
+        if self.ncomp == 2:
+            v[..., :self.N, :] = coefs.astype(self.dtype)
+        else:
+            v[..., :self.N] = coefs.astype(self.dtype)
+
+    def eval_ld(self, pos, form=3):
+        f = getattr(ref_lib(), f"eval_multi_UBspline_{self.dims}d_{self.kind}{LD_SUFFIX[form]}")
+
+        def call(v, g, lh, l2, x, y):
+            xy = (x,) if self.dims == 1 else (x, y)
+            bufs = [ptr(v), ptr(g), ptr(lh)][:1 + min(form, 2)]
+            f(self.p, *xy, *bufs)
+        return _eval_ld(call, self.dims, form, pos, self.dtype, self.N, self.ncomp)
+
+    def __del__(self):
+        try:
+            ref_lib().destroy_Bspline(C.cast(self.p, C.c_void_p))
+        except Exception:
+            pass
 
 
 class RefSpline:

@@ -2,10 +2,11 @@
 library (oracle/_ref/libeinspline_ref.so, built from the reference sources by
 ``make -C oracle ref``).
 
-Each case stores the seeded input data, the table the reference's
+Each 3D case stores the seeded input data, the table the reference's
 set_multi_UBspline_3d_* produced (its float solve for s/c, double for d/z),
-evaluation points, and the reference's eval_multi_UBspline_3d_* and
-eval_multi_UBspline_3d_*_vgh outputs at those points.  The tests then pin the
+evaluation points, and the reference's eval_multi_UBspline_3d_*, _vgh and
+_vghgh outputs at those points.  The ld1_*/ld2_* cases do the same for the
+1D and 2D multi-splines (value, vg, vgl and vgh forms).  The tests then pin the
 oracle against these vectors on machines where the reference cannot be built.
 
 Run from the repository root:  python tests/golden/make_golden.py
@@ -57,10 +58,41 @@ def make_case(name, kind, grids, bcs, N, npts, seed):
     pos = synth.points_uniform(seed + 1, npts, lo, hi)
     v0, _, _ = R.eval(pos, vgh=False)
     v, g, h = R.eval(pos, vgh=True)
+    t3 = R.eval_vghgh(pos[:8])
     bc_arr = np.array([list(b) + [0.0] * (6 - len(b)) for b in bcs], dtype=np.float64)
     return dict(kind=np.array(kind), grids=np.array(grids, dtype=np.float64), bcs=bc_arr,
                 num_splines=np.array(N), data=data, table=R.table(), pos=pos,
-                value=v0, vals=v, grads=g, hess=h)
+                value=v0, vals=v, grads=g, hess=h,
+                vghgh_vals=t3[0], vghgh_grads=t3[1], vghgh_hess=t3[2], vghgh_gradhess=t3[3])
+
+
+# 1D and 2D multi-splines: (name, kind, grids, bcs, num_splines, npts)
+LD_CASES = [
+    ("ld1_s_periodic", "s", [(0.0, 1.0, 11)], [(P, P)], 6, 24),
+    ("ld1_d_mixed", "d", [(-0.4, 1.2, 9)], [(NA, D1, 0.0, 0.0, 0.6, 0.0)], 5, 24),
+    ("ld1_z_anti", "z", [(0.0, 2.0, 8)], [(AP, AP)], 3, 20),
+    ("ld2_c_periodic", "c", [(0.0, 1.0, 8), (0.0, 1.0, 7)], [(P, P)] * 2, 3, 20),
+    ("ld2_d_mixed", "d", [(0.2, 1.4, 7), (-1.0, 0.5, 9)], [(D2, FL, 0.3, 0.0, 0.0, 0.0), (AP, AP)], 4, 24),
+    ("ld2_s_mixed", "s", [(0.0, 1.5, 9), (0.0, 1.0, 6)], [(FL, NA), (P, P)], 5, 24),
+]
+
+
+def make_ld_case(kind, grids, bcs, N, npts, seed):
+    R = O.RefSplineLD(kind, grids, bcs, N)
+    M = tuple(g[2] for g in grids)
+    dt = np.float32 if kind in "sc" else np.float64
+    data = synth.grid_data_uniform(seed, M, N, dt, complex_=kind in "cz")
+    for i in range(N):
+        R.set_spline(i, data[i])
+    pos = synth.points_uniform(seed + 1, npts, [g[0] for g in grids], [g[1] for g in grids])
+    out = {}
+    for form in range(4):
+        for key, arr in zip(("v", "g", "lh"), R.eval_ld(pos, form)):
+            if arr is not None:
+                out[f"f{form}_{key}"] = arr
+    bc_arr = np.array([list(b) + [0.0] * (6 - len(b)) for b in bcs], dtype=np.float64)
+    return dict(kind=np.array(kind), grids=np.array(grids, dtype=np.float64), bcs=bc_arr,
+                num_splines=np.array(N), data=data, table=R.table(), pos=pos, **out)
 
 
 def main():
@@ -68,6 +100,10 @@ def main():
         sys.exit("reference library missing: run `make -C oracle ref` first")
     for k, (name, kind, grids, bcs, N, npts) in enumerate(CASES):
         case = make_case(name, kind, grids, bcs, N, npts, seed=1000 + 17 * k)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **case)
+        print("wrote", name)
+    for k, (name, kind, grids, bcs, N, npts) in enumerate(LD_CASES):
+        case = make_ld_case(kind, grids, bcs, N, npts, seed=2000 + 19 * k)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **case)
         print("wrote", name)
 

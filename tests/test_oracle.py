@@ -8,7 +8,10 @@ import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+GOLDEN = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                if not os.path.basename(p).startswith("ld"))
+GOLDEN_LD = sorted(glob.glob(os.path.join(HERE, "golden", "ld*.npz")))
+REF_BUILT = os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libeinspline_ref.so"))
 
 
 def _load(path):
@@ -20,7 +23,7 @@ def _load(path):
 
 
 def test_golden_present():
-    assert len(GOLDEN) == 8
+    assert len(GOLDEN) == 8 and len(GOLDEN_LD) == 6
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
@@ -120,3 +123,63 @@ def test_det_oracle_algebra(orc):
     assert np.abs(Ai2 - np.linalg.inv(A2)).max() <= 1e-12 * np.abs(Ai2).max()
     r, _, _ = orc.det_ratio(u[None], None, None, Ai[None], k)
     assert abs(r[0] - np.linalg.det(A2) / np.linalg.det(A)) <= 1e-12 * abs(r[0])
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_vghgh(orc, path):
+    """Third derivatives (the std backend's eval_multi_UBspline_3d_*_vghgh)
+    on the reference's own table, bit for bit."""
+    kind, grids, bcs, N, z = _load(path)
+    T = orc.Table(kind, grids, bcs, N)
+    got = T.eval_vghgh(z["pos"][:8], coefs=np.ascontiguousarray(z["table"]))
+    for a, key in zip(got, ("vals", "grads", "hess", "gradhess")):
+        assert np.array_equal(a, z["vghgh_" + key])
+
+
+@pytest.mark.parametrize("path", GOLDEN_LD, ids=[os.path.basename(p)[:-4] for p in GOLDEN_LD])
+def test_golden_lowdim(orc, path):
+    """1D/2D multi-splines: the FP64 solve (d/z bit-identical, s/c to float
+    rounding) and every evaluation form on the reference's table."""
+    kind, grids, bcs, N, z = _load(path)
+    T = orc.Table(kind, grids, bcs, N)
+    for i in range(N):
+        T.set_spline(i, z["data"][i])
+    ref = z["table"]
+    if kind in "dz":
+        assert np.array_equal(T.coefs64, ref)
+    else:
+        assert np.abs(T.coefs64 - ref).max() / np.abs(ref).max() < 1e-6
+    table = np.ascontiguousarray(ref)
+    for form in range(4):
+        got = T.eval_ld(z["pos"], form, coefs=table)
+        for key, a in zip(("v", "g", "lh"), got):
+            if a is not None:
+                assert np.array_equal(a, z[f"f{form}_{key}"]), (form, key)
+
+
+@pytest.mark.skipif(not REF_BUILT, reason="reference library not built here (make -C oracle ref)")
+@pytest.mark.parametrize("kind", "sdcz")
+def test_live_reference_lowdim(orc, kind):
+    """1D and 2D create/set/eval against the live reference, every BC family
+    and evaluation form."""
+    from einspline_gb300 import synth
+    P, NA, D1, D2, FL, AP = orc.PERIODIC, orc.NATURAL, orc.DERIV1, orc.DERIV2, orc.FLAT, orc.ANTIPERIODIC
+    cases = [([(0.0, 1.3, 9)], [(P, P)]), ([(-0.5, 0.7, 11)], [(NA, D1, 0.0, 0.0, 0.3, -0.2)]),
+             ([(0.1, 1.0, 8)], [(AP, AP)]), ([(0.0, 1.3, 9), (-0.5, 0.7, 7)], [(P, P)] * 2),
+             ([(0.0, 1.3, 9), (-0.5, 0.7, 7)], [(D2, FL, 0.5, 0.1, 0.0, 0.0), (AP, AP)])]
+    for grids, bcs in cases:
+        N = 5
+        T = orc.Table(kind, grids, bcs, N)
+        R = orc.RefSplineLD(kind, grids, bcs, N)
+        data = synth.grid_data_uniform(3, T.M[:len(grids)], N, np.float64, complex_=kind in "cz")
+        for i in range(N):
+            T.set_spline(i, data[i])
+            R.set_spline(i, data[i])
+        if kind in "dz":
+            assert np.array_equal(T.coefs64, R.table())
+        R.load_table(T.coefs)
+        pos = synth.points_uniform(5, 16, [g[0] for g in grids], [g[1] for g in grids])
+        for form in range(4):
+            for a, b in zip(T.eval_ld(pos, form), R.eval_ld(pos, form)):
+                if a is not None:
+                    assert np.array_equal(a, b)
