@@ -59,6 +59,20 @@ def _host_struct(kind):
 HOST_STRUCTS = {k: _host_struct(k) for k in "sdcz"}
 
 
+def _host_struct_ld(kind, dims):
+    ax = "xy"[:dims]
+    fields = [("spcode", C.c_int), ("tcode", C.c_int), ("coefs", C.c_void_p)]
+    fields += [(f"{a}_stride", C.c_ssize_t) for a in ax] + [(f"{a}_grid", Ugrid) for a in ax]
+    fields += [(f"{a}BC", BC_TYPES[kind]) for a in ax] + [("num_splines", C.c_int)]
+    if dims == 2 and kind in "cz":
+        fields.append(("lapl2", C.c_void_p))
+    fields.append(("gb300", C.c_void_p))
+    return type(f"multi_UBspline_{dims}d_{kind}", (C.Structure,), {"_fields_": fields})
+
+
+HOST_STRUCTS_LD = {(k, d): _host_struct_ld(k, d) for k in "sdcz" for d in (1, 2)}
+
+
 class uint3(C.Structure):
     _fields_ = [("x", C.c_uint), ("y", C.c_uint), ("z", C.c_uint)]
 
@@ -79,6 +93,16 @@ def _cuda_struct(kind):
 
 
 CUDA_STRUCTS = {k: _cuda_struct(k) for k in "sdcz"}
+
+
+def _cuda_struct_1d(kind):
+    g = C.c_float if kind in "sc" else C.c_double
+    fields = [("coefs", C.c_void_p), ("stride", C.c_uint), ("gridInv", g), ("num_splines", C.c_int),
+              ("dim", C.c_int), ("gb300", C.c_void_p)]
+    return type(f"multi_UBspline_1d_{kind}_cuda", (C.Structure,), {"_fields_": fields})
+
+
+CUDA_STRUCTS_1D = {k: _cuda_struct_1d(k) for k in "sdcz"}
 
 
 class EvalOpts(C.Structure):
@@ -129,6 +153,28 @@ def _signatures():
         sig[f"destroy_multi_UBspline_3d_{k}_cuda"] = ([D], None)
         sig[f"eval_multi_multi_UBspline_3d_{k}_cuda"] = ([D, vp, vp, i32], None)
         sig[f"eval_multi_multi_UBspline_3d_{k}_vgh_cuda"] = ([D, vp, vp, vp, vp, i32], None)
+    for k in "sdcz":
+        BC = BC_TYPES[k]
+        H1 = C.POINTER(HOST_STRUCTS_LD[(k, 1)])
+        H2 = C.POINTER(HOST_STRUCTS_LD[(k, 2)])
+        D1 = C.POINTER(CUDA_STRUCTS_1D[k])
+        sig[f"create_multi_UBspline_1d_{k}"] = ([Ugrid, BC, i32], H1)
+        sig[f"create_multi_UBspline_2d_{k}"] = ([Ugrid, Ugrid, BC, BC, i32], H2)
+        sig[f"set_multi_UBspline_1d_{k}"] = ([H1, i32, vp], None)
+        sig[f"set_multi_UBspline_2d_{k}"] = ([H2, i32, vp], None)
+        for nout, suf in ((1, ""), (2, "_vg"), (3, "_vgl"), (3, "_vgh")):
+            sig[f"eval_multi_UBspline_1d_{k}{suf}"] = ([H1, dbl] + [vp] * nout, None)
+            sig[f"eval_multi_UBspline_2d_{k}{suf}"] = ([H2, dbl, dbl] + [vp] * nout, None)
+        sig[f"create_multi_UBspline_1d_{k}_cuda"] = ([H1], D1)
+        sig[f"destroy_multi_UBspline_1d_{k}_cuda"] = ([D1], None)
+        sig[f"eval_multi_multi_UBspline_1d_{k}_cuda"] = ([D1, vp, vp, i32], None)
+        sig[f"eval_multi_multi_UBspline_1d_{k}_vgl_cuda"] = ([D1, vp, vp, vp, vp, i32], None)
+    sig["create_multi_UBspline_1d_s_cuda_conv"] = ([C.POINTER(HOST_STRUCTS_LD[("d", 1)])],
+                                                   C.POINTER(CUDA_STRUCTS_1D["s"]))
+    sig["create_multi_UBspline_1d_c_cuda_conv"] = ([C.POINTER(HOST_STRUCTS_LD[("z", 1)])],
+                                                   C.POINTER(CUDA_STRUCTS_1D["c"]))
+    sig["set_multi_UBspline_1d_d_BC"] = ([C.POINTER(HOST_STRUCTS_LD[("d", 1)]), i32, vp, BCtype_d], None)
+    sig["set_multi_UBspline_1d_z_BC"] = ([C.POINTER(HOST_STRUCTS_LD[("z", 1)]), i32, vp, BCtype_z], None)
     sig["create_multi_UBspline_3d_s_cuda_conv"] = ([C.POINTER(HOST_STRUCTS["d"])], C.POINTER(CUDA_STRUCTS["s"]))
     sig["create_multi_UBspline_3d_c_cuda_conv"] = ([C.POINTER(HOST_STRUCTS["z"])], C.POINTER(CUDA_STRUCTS["c"]))
     sig["eval_multi_multi_UBspline_3d_s_sign_cuda"] = ([C.POINTER(CUDA_STRUCTS["s"]), vp, vp, vp, i32], None)

@@ -452,6 +452,147 @@ class Server:
             pass
 
 
+class MultiUBsplineLD:
+    """A uniform 1D or 2D multi-spline: create/set/eval_multi_UBspline_{1,2}d_*
+    (src/multi_bspline_create.c:88-248, src/multi_bspline_eval_std_s_impl.h:38-480).
+    grids and bcs hold one or two axes."""
+
+    def __init__(self, kind: str, grids, bcs, num_splines: int):
+        lib = _lib()
+        self.kind, self.N, self.dims = kind, num_splines, len(grids)
+        assert self.dims in (1, 2)
+        self.ncomp = 2 if kind in "cz" else 1
+        self.M = tuple(int(g[2]) for g in grids)
+        ug = [L.Ugrid(float(g[0]), float(g[1]), int(g[2]), 0.0, 0.0) for g in grids]
+        bc = [_bc(kind, b) for b in bcs]
+        p = getattr(lib, f"create_multi_UBspline_{self.dims}d_{kind}")(*ug, *bc, num_splines)
+        check()
+        if not p:
+            raise EinsplineError("create failed")
+        self.ptr = p
+        self.table = C.c_void_p(p.contents.gb300)
+
+    def set(self, i: int, data) -> None:
+        dt = np.float32 if self.kind in "sc" else np.float64
+        d = np.asarray(data)
+        if self.ncomp == 2 and np.iscomplexobj(d):
+            d = np.stack([d.real, d.imag], axis=-1)
+        d = np.ascontiguousarray(d, dtype=dt)
+        getattr(_lib(), f"set_multi_UBspline_{self.dims}d_{self.kind}")(self.ptr, i, d.ctypes.data)
+        check()
+
+    def set_bc(self, i: int, data, bc) -> None:
+        """set_multi_UBspline_1d_{d,z}_BC: spline i solved with its own x BC."""
+        d = np.asarray(data)
+        if self.ncomp == 2 and np.iscomplexobj(d):
+            d = np.stack([d.real, d.imag], axis=-1)
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        getattr(_lib(), f"set_multi_UBspline_1d_{self.kind}_BC")(self.ptr, i, d.ctypes.data, _bc(self.kind, bc))
+        check()
+
+    def flush(self) -> None:
+        _lib().einspline_gb300_flush(self.table)
+        check()
+
+    def table_values(self) -> np.ndarray:
+        """The stored table as float64 [Nx](, Ny) [N] (complex: trailing 2)."""
+        ti = L.TableInfo()
+        lib = _lib()
+        lib.einspline_gb300_get_table_info(self.table, C.byref(ti))
+        check()
+        dt = np.float32 if ti.storage == STORE_F32 else np.float64
+        out = np.empty((ti.nx, ti.ny, ti.nz, ti.ncol_pad), dtype=dt)
+        lib.einspline_gb300_copy_table(self.table, out.ctypes.data, None)
+        check()
+        v = out[..., :ti.ncol].astype(np.float64).reshape((ti.nx, ti.ny)[:self.dims] + (ti.ncol,))
+        return v.reshape(v.shape[:-1] + (self.N, 2)) if self.ncomp == 2 else v
+
+    def eval_point(self, x: float, y: float = 0.0, form: int = 3):
+        """eval_multi_UBspline_{1,2}d_*[_vg|_vgl|_vgh] (form 0..3): (vals,
+        grads, lh) in the CPU layouts; lh is the second derivative (1D), the
+        laplacian (2D vgl) or the Hessian [N][2][2] (2D vgh)."""
+        dt = out_dtype(self.kind)
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((self.N,) + ext, dt)
+        g = np.zeros((self.N,) + ((2,) if self.dims == 2 else ()) + ext, dt)
+        lh = np.zeros((self.N,) + ((2, 2) if self.dims == 2 and form == 3 else ()) + ext, dt)
+        suf = ("", "_vg", "_vgl", "_vgh")[form]
+        f = getattr(_lib(), f"eval_multi_UBspline_{self.dims}d_{self.kind}{suf}")
+        xy = (x,) if self.dims == 1 else (x, y)
+        bufs = [v.ctypes.data, g.ctypes.data, lh.ctypes.data][:1 + min(form, 2)]
+        f(self.ptr, *xy, *bufs)
+        check()
+        return v, (g if form >= 1 else None), (lh if form >= 2 else None)
+
+    def to_cuda(self, conv: bool = False) -> "CudaSpline1D":
+        """create_multi_UBspline_1d_*_cuda (conv: the d->s / z->c _conv forms)."""
+        assert self.dims == 1
+        lib = _lib()
+        if conv:
+            kind = {"d": "s", "z": "c"}[self.kind]
+            p = getattr(lib, f"create_multi_UBspline_1d_{kind}_cuda_conv")(self.ptr)
+        else:
+            kind = self.kind
+            p = getattr(lib, f"create_multi_UBspline_1d_{kind}_cuda")(self.ptr)
+        check()
+        return CudaSpline1D(kind, p, self.N)
+
+    def destroy(self) -> None:
+        if getattr(self, "ptr", None):
+            _lib().destroy_Bspline(C.cast(self.ptr, C.c_void_p))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class CudaSpline1D:
+    """A device handle from create_multi_UBspline_1d_*_cuda[_conv]."""
+
+    def __init__(self, kind, ptr, N):
+        self.kind, self.ptr, self.N = kind, ptr, N
+        self.ncomp = 2 if kind in "cz" else 1
+
+    @property
+    def fields(self):
+        return self.ptr.contents
+
+    def eval_multi(self, pos, vgl=False):
+        """eval_multi_multi_UBspline_1d_*[_vgl]_cuda: pos [P] (float for s/c,
+        double for d/z) -> vals, grads, lapl [P, N * ncomp] (derivatives with
+        respect to the cell coordinate, as the reference's kernels)."""
+        torch = _torch()
+        P = int(pos.shape[0])
+        dt = torch.float32 if self.kind in "sc" else torch.float64
+        nr = self.N * self.ncomp
+        outs = [torch.zeros((P, nr), dtype=dt, device=pos.device) for _ in range(3 if vgl else 1)]
+        ptrs = [torch.arange(P, dtype=torch.int64, device=pos.device) * (nr * o.element_size()) + o.data_ptr()
+                for o in outs]
+        lib = _lib()
+        if vgl:
+            getattr(lib, f"eval_multi_multi_UBspline_1d_{self.kind}_vgl_cuda")(
+                self.ptr, C.c_void_p(pos.data_ptr()), *[C.c_void_p(q.data_ptr()) for q in ptrs], P)
+        else:
+            getattr(lib, f"eval_multi_multi_UBspline_1d_{self.kind}_cuda")(
+                self.ptr, C.c_void_p(pos.data_ptr()), C.c_void_p(ptrs[0].data_ptr()), P)
+        check()
+        return tuple(outs) if vgl else (outs[0], None, None)
+
+    def destroy(self):
+        if getattr(self, "ptr", None):
+            getattr(_lib(), f"destroy_multi_UBspline_1d_{self.kind}_cuda")(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 class Determinants:
     """A population of walkers' Slater matrices A [W][ld][ld] and inverses
     (torch float32 CUDA tensors, one contiguous block each) for the fused

@@ -95,7 +95,7 @@ __global__ void k_scale_box(double *pos, int64_t n, double lx, double ly, double
 }
 
 static int check_opts(Table *t, const einspline_gb300_eval_opts *o) {
-  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
   if (!o) return fail(EINSPLINE_GB300_EINVAL, "opts is NULL");
   if (o->rule < 0 || o->rule > 1 || o->layout < 0 || o->layout > 1)
     return fail(EINSPLINE_GB300_EINVAL, "opts.rule and opts.layout must be 0 or 1");
@@ -246,7 +246,7 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
 
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode) {
   clear();
-  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
   if (mode < -1 || mode > 3) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1, 2 or 3");
   t->tile_mode = mode;
   return 0;
@@ -254,7 +254,7 @@ int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode) {
 
 int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb) {
   clear();
-  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
   if (tx == 0 && ty == 0 && pb == 0) { t->tile_tx = t->tile_ty = t->tile_pb = 0; return 0; }
   if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
     return fail(EINSPLINE_GB300_EINVAL, "tile must have tx a multiple of 32, tx*ty <= 256, 1 <= pb <= 64");
@@ -264,20 +264,20 @@ int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb) {
 
 int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb) {
   clear();
-  if (!table_ok(t) || !tx || !ty || !pb) return fail(EINSPLINE_GB300_EINVAL, "bad argument");
+  if (!table3_ok(t) || !tx || !ty || !pb) return fail(EINSPLINE_GB300_EINVAL, "bad argument");
   pick_tile(t, true, 0, *tx, *ty, *pb);
   return 0;
 }
 
 int einspline_gb300_get_load_mode(einspline_gb300_table *t) {
   clear();
-  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
   return pick_mode(t, true);
 }
 
 int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
   clear();
-  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
   if (npts < 1) return fail(EINSPLINE_GB300_EINVAL, "npts must be >= 1");
   if (int r = table_flush(t)) return r;
   const size_t rb = t->storage == ST_F64 ? 8 : 4;

@@ -64,6 +64,34 @@ S *create_host(char kind, type_code tc, Ugrid xg, Ugrid yg, Ugrid zg, BC xb, BC 
   return s;
 }
 
+// 1D and 2D host structs (src/multi_bspline_create.c:88-150, :152-248 and
+// the d/c/z counterparts): the first DIMS axes of a table.
+template <typename S, int DIMS, typename BC, typename V>
+S *create_host_ld(char kind, type_code tc, const Ugrid *ug, const BC *bc, int n) {
+  clear();
+  GridDesc g[3];
+  for (int a = 0; a < DIMS; a++) g[a] = make_axis(ug[a], bc[a]);
+  Table *t = table_create(kind, g, n, ST_NATIVE, DIMS);
+  if (!t) return nullptr;
+  S *s = (S *)calloc(1, sizeof(S));
+  if (!s) { table_destroy(t); fail(EINSPLINE_GB300_ENOMEM, "out of host memory"); return nullptr; }
+  s->spcode = DIMS == 1 ? MULTI_U1D : MULTI_U2D;
+  s->tcode = tc;
+  s->coefs = (V *)t->coefs;
+  const int per = t->ncomp;
+  s->x_stride = (intptr_t)(t->xs / per);
+  fill_grid(s->x_grid, t, 0);
+  s->xBC = bc[0];
+  if constexpr (DIMS == 2) {
+    s->y_stride = (intptr_t)(t->ys / per);
+    fill_grid(s->y_grid, t, 1);
+    s->yBC = bc[1];
+  }
+  s->num_splines = n;
+  s->gb300 = t;
+  return s;
+}
+
 template <typename S>
 Table *table_of(S *s, const char *fn) {
   if (!s || !table_ok(s->gb300)) {
@@ -98,6 +126,33 @@ CS *make_cuda(Table *src, int storage, bool is_double_grid) {
   c->gb300 = t;
   (void)is_double_grid;
   return c;
+}
+
+// 1D *_cuda handles (src/multi_bspline_create_cuda.cu:17-125): a private
+// device copy; stride in reals, dim = number of cells.
+template <typename CS, typename G>
+CS *make_cuda_1d(Table *src, int storage) {
+  Table *t = table_clone(src, storage);
+  if (!t) return nullptr;
+  CS *c = (CS *)calloc(1, sizeof(CS));
+  if (!c) { table_destroy(t); fail(EINSPLINE_GB300_ENOMEM, "out of host memory"); return nullptr; }
+  c->coefs = (decltype(c->coefs))t->coefs;
+  c->stride = (t->xs > 0xFFFFFFFFll) ? 0u : (unsigned)t->xs;
+  c->gridInv = (G)t->dinv[0];
+  c->num_splines = t->num_splines;
+  c->dim = t->Nc[0] - 3;
+  c->gb300 = t;
+  return c;
+}
+
+template <typename S>
+Table *table_of_dims(S *s, int dims, const char *fn) {
+  Table *t = table_of(s, fn);
+  if (t && t->dims != dims) {
+    fail(EINSPLINE_GB300_EINVAL, "%s: the spline is not %dD", fn, dims);
+    return nullptr;
+  }
+  return t;
 }
 
 template <typename CS>
@@ -165,17 +220,24 @@ void set_multi_UBspline_3d_z(multi_UBspline_3d_z *s, int num, complex_double *da
 
 void destroy_multi_UBspline(Bspline *spline) {
   if (!spline) return;
-  if (spline->sp_code != MULTI_U3D) {
-    fail(EINSPLINE_GB300_EINVAL, "destroy_multi_UBspline: only uniform 3D multi-splines are built here");
-    return;
-  }
   Table *t = nullptr;
-  switch (spline->t_code) {
-    case SINGLE_REAL: t = ((multi_UBspline_3d_s *)spline)->gb300; break;
-    case DOUBLE_REAL: t = ((multi_UBspline_3d_d *)spline)->gb300; break;
-    case SINGLE_COMPLEX: t = ((multi_UBspline_3d_c *)spline)->gb300; break;
-    case DOUBLE_COMPLEX: t = ((multi_UBspline_3d_z *)spline)->gb300; break;
+  const int tc = spline->t_code;
+#define EG_HANDLE(D)                                                             \
+  switch (tc) {                                                                  \
+    case SINGLE_REAL: t = ((multi_UBspline_##D##_s *)spline)->gb300; break;      \
+    case DOUBLE_REAL: t = ((multi_UBspline_##D##_d *)spline)->gb300; break;      \
+    case SINGLE_COMPLEX: t = ((multi_UBspline_##D##_c *)spline)->gb300; break;   \
+    case DOUBLE_COMPLEX: t = ((multi_UBspline_##D##_z *)spline)->gb300; break;   \
   }
+  switch (spline->sp_code) {
+    case MULTI_U1D: EG_HANDLE(1d) break;
+    case MULTI_U2D: EG_HANDLE(2d) break;
+    case MULTI_U3D: EG_HANDLE(3d) break;
+    default:
+      fail(EINSPLINE_GB300_EINVAL, "destroy_multi_UBspline: only uniform 1D/2D/3D multi-splines are built here");
+      return;
+  }
+#undef EG_HANDLE
   if (table_ok(t)) table_destroy(t);
   free(spline);
 }
@@ -238,6 +300,115 @@ void destroy_multi_UBspline_3d_s_cuda(multi_UBspline_3d_s_cuda *c) { destroy_cud
 void destroy_multi_UBspline_3d_c_cuda(multi_UBspline_3d_c_cuda *c) { destroy_cuda(c); }
 void destroy_multi_UBspline_3d_d_cuda(multi_UBspline_3d_d_cuda *c) { destroy_cuda(c); }
 void destroy_multi_UBspline_3d_z_cuda(multi_UBspline_3d_z_cuda *c) { destroy_cuda(c); }
+
+multi_UBspline_1d_s *create_multi_UBspline_1d_s(Ugrid x, BCtype_s xb, int num_splines) {
+  return create_host_ld<multi_UBspline_1d_s, 1, BCtype_s, float>('s', SINGLE_REAL, &x, &xb, num_splines);
+}
+multi_UBspline_2d_s *create_multi_UBspline_2d_s(Ugrid x, Ugrid y, BCtype_s xb, BCtype_s yb, int num_splines) {
+  const Ugrid g[2] = {x, y};
+  const BCtype_s b[2] = {xb, yb};
+  return create_host_ld<multi_UBspline_2d_s, 2, BCtype_s, float>('s', SINGLE_REAL, g, b, num_splines);
+}
+void set_multi_UBspline_1d_s(multi_UBspline_1d_s *s, int num, float *data) {
+  set_host(s, num, data, "set_multi_UBspline_1d_s");
+}
+void set_multi_UBspline_2d_s(multi_UBspline_2d_s *s, int num, float *data) {
+  set_host(s, num, data, "set_multi_UBspline_2d_s");
+}
+multi_UBspline_1d_d *create_multi_UBspline_1d_d(Ugrid x, BCtype_d xb, int num_splines) {
+  return create_host_ld<multi_UBspline_1d_d, 1, BCtype_d, double>('d', DOUBLE_REAL, &x, &xb, num_splines);
+}
+multi_UBspline_2d_d *create_multi_UBspline_2d_d(Ugrid x, Ugrid y, BCtype_d xb, BCtype_d yb, int num_splines) {
+  const Ugrid g[2] = {x, y};
+  const BCtype_d b[2] = {xb, yb};
+  return create_host_ld<multi_UBspline_2d_d, 2, BCtype_d, double>('d', DOUBLE_REAL, g, b, num_splines);
+}
+void set_multi_UBspline_1d_d(multi_UBspline_1d_d *s, int num, double *data) {
+  set_host(s, num, data, "set_multi_UBspline_1d_d");
+}
+void set_multi_UBspline_2d_d(multi_UBspline_2d_d *s, int num, double *data) {
+  set_host(s, num, data, "set_multi_UBspline_2d_d");
+}
+multi_UBspline_1d_c *create_multi_UBspline_1d_c(Ugrid x, BCtype_c xb, int num_splines) {
+  return create_host_ld<multi_UBspline_1d_c, 1, BCtype_c, complex_float>('c', SINGLE_COMPLEX, &x, &xb, num_splines);
+}
+multi_UBspline_2d_c *create_multi_UBspline_2d_c(Ugrid x, Ugrid y, BCtype_c xb, BCtype_c yb, int num_splines) {
+  const Ugrid g[2] = {x, y};
+  const BCtype_c b[2] = {xb, yb};
+  return create_host_ld<multi_UBspline_2d_c, 2, BCtype_c, complex_float>('c', SINGLE_COMPLEX, g, b, num_splines);
+}
+void set_multi_UBspline_1d_c(multi_UBspline_1d_c *s, int num, complex_float *data) {
+  set_host(s, num, data, "set_multi_UBspline_1d_c");
+}
+void set_multi_UBspline_2d_c(multi_UBspline_2d_c *s, int num, complex_float *data) {
+  set_host(s, num, data, "set_multi_UBspline_2d_c");
+}
+multi_UBspline_1d_z *create_multi_UBspline_1d_z(Ugrid x, BCtype_z xb, int num_splines) {
+  return create_host_ld<multi_UBspline_1d_z, 1, BCtype_z, complex_double>('z', DOUBLE_COMPLEX, &x, &xb, num_splines);
+}
+multi_UBspline_2d_z *create_multi_UBspline_2d_z(Ugrid x, Ugrid y, BCtype_z xb, BCtype_z yb, int num_splines) {
+  const Ugrid g[2] = {x, y};
+  const BCtype_z b[2] = {xb, yb};
+  return create_host_ld<multi_UBspline_2d_z, 2, BCtype_z, complex_double>('z', DOUBLE_COMPLEX, g, b, num_splines);
+}
+void set_multi_UBspline_1d_z(multi_UBspline_1d_z *s, int num, complex_double *data) {
+  set_host(s, num, data, "set_multi_UBspline_1d_z");
+}
+void set_multi_UBspline_2d_z(multi_UBspline_2d_z *s, int num, complex_double *data) {
+  set_host(s, num, data, "set_multi_UBspline_2d_z");
+}
+// src/multi_bspline_create.c:830-836 (d) and the z counterpart: one spline
+// solved with its own x boundary condition (codes of the same periodicity as
+// the table's).
+void set_multi_UBspline_1d_d_BC(multi_UBspline_1d_d *s, int num, double *data, BCtype_d xBC) {
+  clear();
+  Table *t = table_of_dims(s, 1, "set_multi_UBspline_1d_d_BC");
+  if (!t) return;
+  const double lv[2] = {xBC.lVal, 0.0}, rv[2] = {xBC.rVal, 0.0};
+  table_set_bc(t, num, data, xBC.lCode, xBC.rCode, lv, rv);
+}
+void set_multi_UBspline_1d_z_BC(multi_UBspline_1d_z *s, int num, complex_double *data, BCtype_z xBC) {
+  clear();
+  Table *t = table_of_dims(s, 1, "set_multi_UBspline_1d_z_BC");
+  if (!t) return;
+  const double lv[2] = {xBC.lVal_r, xBC.lVal_i}, rv[2] = {xBC.rVal_r, xBC.rVal_i};
+  table_set_bc(t, num, data, xBC.lCode, xBC.rCode, lv, rv);
+}
+
+multi_UBspline_1d_s_cuda *create_multi_UBspline_1d_s_cuda(multi_UBspline_1d_s *s) {
+  clear();
+  Table *t = table_of_dims(s, 1, "create_multi_UBspline_1d_s_cuda");
+  return t ? make_cuda_1d<multi_UBspline_1d_s_cuda, float>(t, ST_NATIVE) : nullptr;
+}
+multi_UBspline_1d_s_cuda *create_multi_UBspline_1d_s_cuda_conv(multi_UBspline_1d_d *s) {
+  clear();
+  Table *t = table_of_dims(s, 1, "create_multi_UBspline_1d_s_cuda_conv");
+  return t ? make_cuda_1d<multi_UBspline_1d_s_cuda, float>(t, ST_F32) : nullptr;
+}
+multi_UBspline_1d_c_cuda *create_multi_UBspline_1d_c_cuda(multi_UBspline_1d_c *s) {
+  clear();
+  Table *t = table_of_dims(s, 1, "create_multi_UBspline_1d_c_cuda");
+  return t ? make_cuda_1d<multi_UBspline_1d_c_cuda, float>(t, ST_NATIVE) : nullptr;
+}
+multi_UBspline_1d_c_cuda *create_multi_UBspline_1d_c_cuda_conv(multi_UBspline_1d_z *s) {
+  clear();
+  Table *t = table_of_dims(s, 1, "create_multi_UBspline_1d_c_cuda_conv");
+  return t ? make_cuda_1d<multi_UBspline_1d_c_cuda, float>(t, ST_F32) : nullptr;
+}
+multi_UBspline_1d_d_cuda *create_multi_UBspline_1d_d_cuda(multi_UBspline_1d_d *s) {
+  clear();
+  Table *t = table_of_dims(s, 1, "create_multi_UBspline_1d_d_cuda");
+  return t ? make_cuda_1d<multi_UBspline_1d_d_cuda, double>(t, ST_NATIVE) : nullptr;
+}
+multi_UBspline_1d_z_cuda *create_multi_UBspline_1d_z_cuda(multi_UBspline_1d_z *s) {
+  clear();
+  Table *t = table_of_dims(s, 1, "create_multi_UBspline_1d_z_cuda");
+  return t ? make_cuda_1d<multi_UBspline_1d_z_cuda, double>(t, ST_NATIVE) : nullptr;
+}
+void destroy_multi_UBspline_1d_s_cuda(multi_UBspline_1d_s_cuda *c) { destroy_cuda(c); }
+void destroy_multi_UBspline_1d_c_cuda(multi_UBspline_1d_c_cuda *c) { destroy_cuda(c); }
+void destroy_multi_UBspline_1d_d_cuda(multi_UBspline_1d_d_cuda *c) { destroy_cuda(c); }
+void destroy_multi_UBspline_1d_z_cuda(multi_UBspline_1d_z_cuda *c) { destroy_cuda(c); }
 
 // ------------------------------------------------------------ extensions
 int einspline_gb300_set_3d_device(einspline_gb300_table *t, int first, int count, const void *data_d) {

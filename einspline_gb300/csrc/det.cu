@@ -387,7 +387,7 @@ int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_de
                               float *lapl_d, float *const *row_d, void *stream) {
   static const char *fn = "einspline_gb300_det_ratio";
   clear();
-  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "%s: bad table handle", fn);
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "%s: bad table handle", fn);
   if (int r = check_det_opts(o, fn)) return r;
   if (t->ncomp != 1 || t->storage == ST_F64)
     return fail(EINSPLINE_GB300_EINVAL, "%s: real float tables only (s kind, any float/16-bit storage)", fn);

@@ -68,6 +68,8 @@ void pack_line_factors(const LineFactors &f, std::vector<double> &out);
 struct einspline_gb300_table {
   uint32_t magic = eg::kMagic;
   char kind = 's';        // 's','d','c','z'
+  int dims = 3;           // 1, 2 or 3 axes (1D/2D/3D multi-splines); axes
+                          // beyond dims hold one point and one coefficient
   int storage = eg::ST_F32;
   int ncomp = 1;          // 1 real, 2 complex
   int num_splines = 0;
@@ -134,16 +136,23 @@ struct GridDesc {
   double lval[2], rval[2];
 };
 
-// Creates a table object with its device storage (zero-filled).
-Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage);
+// Creates a table object with its device storage (zero-filled).  Only the
+// first dims entries of g are read.
+Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage, int dims = 3);
 void table_destroy(Table *t);
 // Copy of src converted to another storage (device to device), with new
 // private storage; used by the *_cuda creators.
 Table *table_clone(Table *src, int storage);
 // Queue set calls; data on host (from_device=0) or device.
 int table_set(Table *t, int first, int count, const void *data, bool from_device);
+// One spline of a 1D table solved with its own x boundary condition
+// (set_multi_UBspline_1d_{d,z}_BC); host data.
+int table_set_bc(Table *t, int spline, const void *data, int lcode, int rcode, const double lval[2],
+                 const double rval[2]);
 int table_flush(Table *t);
 inline bool table_ok(const Table *t) { return t && t->magic == kMagic; }
+// A 3D table: what every 3D entry point and extension takes.
+inline bool table3_ok(const Table *t) { return table_ok(t) && t->dims == 3; }
 
 // ---------------------------------------------------------------- eval
 struct EvalArgs {
@@ -179,16 +188,20 @@ struct EvalArgs {
                               // 2 vgl (CPU entries): grads and lapl = trace(H) in hess;
                               // 3 vg: value and gradient only
   const void *sign;           // optional per-point factor (output type) on every output
+  int unscaled;               // 1D/2D kernels: derivatives in cell units (no delta_inv),
+                              // as the reference's 1D GPU vgl kernels return them
   const void *linv;           // out 1: 3x3 row-major G (output type)
   int64_t lrow;               // out 1: row stride of the gradient/laplacian rows (reals)
 };
 
 int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb);
+// Device and pinned host scratch of the single-point entries (40 * ncol reals).
+int point_scratch(Table *t, const char *fn);
+void fill_eval_geometry(const Table *t, EvalArgs &a);
 // Kernel, grid, block and shared memory of a launch without launching it
 // (for graph kernel nodes); fills a.pb and a.ntiles.
 int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *grid,
                  dim3 *block, size_t *smem);
-void fill_eval_geometry(const Table *t, EvalArgs &a);
 void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb);
 // Load mode of launches on this table (see EvalArgs::mode).
 int pick_mode(Table *t, bool vgh);

@@ -604,21 +604,6 @@ void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb) {
   (void)npts;
 }
 
-}  // namespace eg
-
-using namespace eg;
-
-namespace {
-
-template <typename S>
-Table *host_table(S *s, const char *fn) {
-  if (!s || !table_ok(s->gb300)) {
-    fail(EINSPLINE_GB300_EINVAL, "%s: not a spline made by this library", fn);
-    return nullptr;
-  }
-  return s->gb300;
-}
-
 // Device and pinned host scratch for the single-point entries: 40 output
 // reals per column (value, 3 gradient, 9 Hessian, 27 third-derivative).
 int point_scratch(Table *t, const char *fn) {
@@ -633,6 +618,22 @@ int point_scratch(Table *t, const char *fn) {
   }
   return 0;
 }
+
+}  // namespace eg
+
+using namespace eg;
+
+namespace {
+
+template <typename S>
+Table *host_table(S *s, const char *fn) {
+  if (!s || !table3_ok(s->gb300)) {
+    fail(EINSPLINE_GB300_EINVAL, "%s: not a spline made by this library", fn);
+    return nullptr;
+  }
+  return s->gb300;
+}
+
 
 // Single point, host outputs in the CPU layout.  out: 0 vgh, 2 vgl, 3 vg.
 template <typename S, typename V>
@@ -718,7 +719,7 @@ void eval_cuda(CS *c, const void *pos_d, bool pos_f64, void *const *vals_d, void
                void *const *hess_d, int num, bool vgh, const char *fn, int out = 0, const void *sign = nullptr,
                const void *linv = nullptr, int64_t lrow = 0) {
   clear();
-  if (!c || !table_ok(c->gb300)) { fail(EINSPLINE_GB300_EINVAL, "%s: not a handle made by this library", fn); return; }
+  if (!c || !table3_ok(c->gb300)) { fail(EINSPLINE_GB300_EINVAL, "%s: not a handle made by this library", fn); return; }
   if (num <= 0) return;
   Table *t = c->gb300;
   EvalArgs a;

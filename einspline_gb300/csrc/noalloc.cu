@@ -63,7 +63,7 @@ extern "C" int einspline_gb300_eval_3d_sorted_noalloc(einspline_gb300_table *t, 
                                                       int64_t npts, const void *pos_d, void *vals_d, void *grads_d,
                                                       void *hess_d, void *stream) {
   clear();
-  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_eval_3d_sorted_noalloc: bad table handle");
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_eval_3d_sorted_noalloc: bad table handle");
   if (!o || o->rule < 0 || o->rule > 1 || o->layout < 0 || o->layout > 1)
     return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_eval_3d_sorted_noalloc: bad options");
   if (npts < 0) return fail(EINSPLINE_GB300_EINVAL, "npts < 0");

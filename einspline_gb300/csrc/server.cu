@@ -308,7 +308,7 @@ extern "C" {
 
 einspline_gb300_server *einspline_gb300_server_create(einspline_gb300_table *t, const einspline_gb300_server_opts *opts) {
   clear();
-  if (!table_ok(t)) { fail(EINSPLINE_GB300_EINVAL, "bad table handle"); return nullptr; }
+  if (!table3_ok(t)) { fail(EINSPLINE_GB300_EINVAL, "bad table handle"); return nullptr; }
   if (table_flush(t)) return nullptr;
   Server *v = new Server();
   v->t = t;

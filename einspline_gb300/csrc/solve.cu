@@ -397,11 +397,12 @@ static int alloc_storage(Table *t) {
   return 0;
 }
 
-Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage) {
+Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage, int dims) {
   if (num_splines < 1) { fail(EINSPLINE_GB300_EINVAL, "num_splines must be >= 1 (got %d)", num_splines); return nullptr; }
+  if (dims < 1 || dims > 3) { fail(EINSPLINE_GB300_EINVAL, "dims must be 1, 2 or 3"); return nullptr; }
   const int st = resolve_storage(kind, storage);
   if (st < 0) { fail(EINSPLINE_GB300_EINVAL, "storage %d is not available for type %c", storage, kind); return nullptr; }
-  for (int a = 0; a < 3; a++) {
+  for (int a = 0; a < dims; a++) {
     // Only lCode decides between the cyclic and boundary-row systems, as in
     // src/bspline_create.c:1120; rCode matters only for the latter.
     const bool cyc = (g[a].lcode == PERIODIC || g[a].lcode == ANTIPERIODIC);
@@ -424,7 +425,15 @@ Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage
   t->elem_bytes = storage_bytes(st);
   t->in_bytes = (kind == 's' || kind == 'c') ? 4 : 8;
   t->num_splines = num_splines;
-  for (int a = 0; a < 3; a++) {
+  t->dims = dims;
+  for (int a = dims; a < 3; a++) {
+    // an absent axis: one point, one coefficient, never swept or evaluated
+    t->M[a] = 1; t->Nc[a] = 1;
+    t->start[a] = 0.0; t->end[a] = 1.0; t->delta[a] = 1.0; t->dinv[a] = 1.0;
+    t->lcode[a] = t->rcode[a] = -1;
+    for (int p = 0; p < 2; p++) t->lval[a][p] = t->rval[a][p] = 0.0;
+  }
+  for (int a = 0; a < dims; a++) {
     t->M[a] = g[a].num;
     const bool cyc = (g[a].lcode == PERIODIC || g[a].lcode == ANTIPERIODIC);
     t->Nc[a] = cyc ? g[a].num + 3 : g[a].num + 2;
@@ -444,9 +453,9 @@ Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage
     return nullptr;
   }
   if (alloc_storage(t)) { table_destroy(t); return nullptr; }
-  // Line factors for the three axes, packed into one device buffer.
+  // Line factors for the axes, packed into one device buffer.
   std::vector<double> all, one;
-  for (int a = 0; a < 3; a++) {
+  for (int a = 0; a < dims; a++) {
     LineFactors f;
     build_line_factors(t->M[a], t->lcode[a], t->rcode[a], t->dinv[a], f);
     pack_line_factors(f, one);
@@ -519,7 +528,13 @@ static int ensure_work(Table *t) {
   return 0;
 }
 
-static int flush_locked(Table *t) {
+// x-axis override for one flush (set_multi_UBspline_1d_{d,z}_BC).
+struct AxisOverride {
+  const double *fac;  // device line factors
+  double lval[2], rval[2];
+};
+
+static int flush_locked(Table *t, const AxisOverride *ov = nullptr) {
   const int n = (int)t->pend_spline.size();
   if (n == 0) return 0;
   const int nc = t->ncomp;
@@ -545,13 +560,17 @@ static int flush_locked(Table *t) {
   const int64_t az = ncw, ay = (int64_t)Mz * ncw, ax = (int64_t)My * Mz * ncw;
   const int TB = 128;
   const int cblocks = (ncw + TB - 1) / TB;
-  for (int axis = 0; axis < 3; axis++) {
+  for (int axis = 0; axis < t->dims; axis++) {
     SweepArgs a;
     memset(&a, 0, sizeof(a));
     a.fac = t->factors_d + t->factor_off[axis];
     a.ncw = ncw;
     a.ncomp = nc;
     for (int p = 0; p < 2; p++) { a.lval[p] = t->lval[axis][p]; a.rval[p] = t->rval[axis][p]; }
+    if (ov && axis == 0) {
+      a.fac = ov->fac;
+      for (int p = 0; p < 2; p++) { a.lval[p] = ov->lval[p]; a.rval[p] = ov->rval[p]; }
+    }
     if (axis == 0) {
       a.in = t->work_a; a.out = t->work_w;
       a.nv = Mz; a.nlines = (int64_t)My * Mz;
@@ -608,6 +627,56 @@ int table_flush(Table *t) {
   // Evaluations may run on any stream: make the solved table visible to all.
   if (had) EG_CUDA(cudaStreamSynchronize(t->stream));
   return 0;
+}
+
+int table_set_bc(Table *t, int spline, const void *data, int lcode, int rcode, const double lval[2],
+                 const double rval[2]) {
+  if (t->dims != 1) return fail(EINSPLINE_GB300_EINVAL, "a per-spline boundary condition needs a 1D table");
+  if (spline < 0 || spline >= t->num_splines)
+    return fail(EINSPLINE_GB300_EINVAL, "spline %d outside [0, %d)", spline, t->num_splines);
+  if (!data) return fail(EINSPLINE_GB300_EINVAL, "data pointer is NULL");
+  const bool cyc = (lcode == PERIODIC || lcode == ANTIPERIODIC);
+  const bool tcyc = (t->lcode[0] == PERIODIC || t->lcode[0] == ANTIPERIODIC);
+  if (lcode < PERIODIC || lcode > ANTIPERIODIC || cyc != tcyc ||
+      (!cyc && (rcode < DERIV1 || rcode > NATURAL)))
+    return fail(EINSPLINE_GB300_EINVAL,
+                "boundary condition must be valid and periodic exactly when the table's is (the table has %d "
+                "coefficients)", t->Nc[0]);
+  std::lock_guard<std::mutex> g(t->mu);
+  if (int r = ensure_work(t)) return r;
+  if (int r = flush_locked(t)) return r;
+  LineFactors f;
+  build_line_factors(t->M[0], lcode, rcode, t->dinv[0], f);
+  std::vector<double> pk;
+  pack_line_factors(f, pk);
+  double *fac = nullptr;
+  if (cudaMalloc(&fac, pk.size() * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(EINSPLINE_GB300_ENOMEM, "line factors");
+  }
+  AxisOverride ov;
+  ov.fac = fac;
+  for (int p = 0; p < 2; p++) {
+    // FLAT and NATURAL force a zero boundary value (src/bspline_create.c:1137, :1156).
+    ov.lval[p] = (lcode == FLAT || lcode == NATURAL) ? 0.0 : lval[p];
+    ov.rval[p] = (rcode == FLAT || rcode == NATURAL) ? 0.0 : rval[p];
+  }
+  const size_t per = (size_t)t->M[0] * t->ncomp * t->in_bytes;
+  t->pend_spline.push_back(spline);
+  t->slot_of[spline] = 0;
+  int r = 0;
+  if (cudaMemcpyAsync(fac, pk.data(), pk.size() * sizeof(double), cudaMemcpyHostToDevice, t->stream) != cudaSuccess ||
+      cudaMemcpyAsync(t->staging, data, per, cudaMemcpyHostToDevice, t->stream) != cudaSuccess) {
+    r = cuda_check(cudaGetLastError(), "set with boundary condition");
+    t->pend_spline.clear();
+    t->slot_of.clear();
+  } else {
+    r = flush_locked(t, &ov);
+  }
+  cudaError_t e = cudaStreamSynchronize(t->stream);
+  cudaFree(fac);
+  if (!r && e != cudaSuccess) r = cuda_check(e, "set with boundary condition");
+  return r;
 }
 
 int table_set(Table *t, int first, int count, const void *data, bool from_device) {
@@ -676,7 +745,7 @@ Table *table_clone(Table *src, int storage) {
   char kind = src->kind;
   if (storage != ST_F64 && storage != ST_NATIVE && (kind == 'd' || kind == 'z')) kind = (kind == 'd') ? 's' : 'c';
   if (storage == ST_NATIVE) storage = src->storage;
-  Table *t = table_create(kind, g, src->num_splines, storage);
+  Table *t = table_create(kind, g, src->num_splines, storage, src->dims);
   if (!t) return nullptr;
   // Make the copy on the source's stream order, then on the new stream.
   if (cudaStreamSynchronize(src->stream) != cudaSuccess) { cuda_check(cudaGetLastError(), "clone sync"); table_destroy(t); return nullptr; }

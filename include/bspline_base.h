@@ -20,7 +20,7 @@ typedef complex double complex_double;
 
 /* Boundary conditions (src/bspline_base.h:49). */
 typedef enum { PERIODIC, DERIV1, DERIV2, FLAT, NATURAL, ANTIPERIODIC } bc_code;
-/* Spline kinds (src/bspline_base.h:50-53); this library builds MULTI_U3D. */
+/* Spline kinds (src/bspline_base.h:50-53); this library builds MULTI_U1D, MULTI_U2D and MULTI_U3D. */
 typedef enum { U1D, U2D, U3D,
                NU1D, NU2D, NU3D,
                MULTI_U1D, MULTI_U2D, MULTI_U3D,

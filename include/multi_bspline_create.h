@@ -1,7 +1,9 @@
 /*
- * multi_bspline_create.h -- create / set / destroy for uniform 3D multi-splines.
+ * multi_bspline_create.h -- create / set / destroy for uniform 1D, 2D and
+ * 3D multi-splines.
  *
- * Replaces the 3D entries of src/multi_bspline_create.h:51-171
+ * Replaces the entries of src/multi_bspline_create.h:41-171: 1D/2D at
+ * :41-62 (s), :74-101 (d), :109-130 (c), :141-166 (z), and 3D
  * (create_multi_UBspline_3d_{s,d,c,z} at :60-63, :88-91, :120-123, :150-153;
  *  set_multi_UBspline_3d_{s,d,c,z} at :75, :105, :136, :170).
  *
@@ -28,6 +30,36 @@
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+/* ---- 1D and 2D multi-splines (src/multi_bspline_create.c:88-248 s,
+ * :389-575 c, :767-940 d, :1091-1316 z).  Same rules as 3D: FP64 solve on
+ * the GPU, rounded once on store; data is [Mx] or [Mx][My], C order. */
+multi_UBspline_1d_s *create_multi_UBspline_1d_s(Ugrid x_grid, BCtype_s xBC, int num_splines);
+multi_UBspline_2d_s *create_multi_UBspline_2d_s(Ugrid x_grid, Ugrid y_grid, BCtype_s xBC, BCtype_s yBC,
+                                                 int num_splines);
+void set_multi_UBspline_1d_s(multi_UBspline_1d_s *spline, int spline_num, float *data);
+void set_multi_UBspline_2d_s(multi_UBspline_2d_s *spline, int spline_num, float *data);
+multi_UBspline_1d_d *create_multi_UBspline_1d_d(Ugrid x_grid, BCtype_d xBC, int num_splines);
+multi_UBspline_2d_d *create_multi_UBspline_2d_d(Ugrid x_grid, Ugrid y_grid, BCtype_d xBC, BCtype_d yBC,
+                                                 int num_splines);
+void set_multi_UBspline_1d_d(multi_UBspline_1d_d *spline, int spline_num, double *data);
+void set_multi_UBspline_2d_d(multi_UBspline_2d_d *spline, int spline_num, double *data);
+multi_UBspline_1d_c *create_multi_UBspline_1d_c(Ugrid x_grid, BCtype_c xBC, int num_splines);
+multi_UBspline_2d_c *create_multi_UBspline_2d_c(Ugrid x_grid, Ugrid y_grid, BCtype_c xBC, BCtype_c yBC,
+                                                 int num_splines);
+void set_multi_UBspline_1d_c(multi_UBspline_1d_c *spline, int spline_num, complex_float *data);
+void set_multi_UBspline_2d_c(multi_UBspline_2d_c *spline, int spline_num, complex_float *data);
+multi_UBspline_1d_z *create_multi_UBspline_1d_z(Ugrid x_grid, BCtype_z xBC, int num_splines);
+multi_UBspline_2d_z *create_multi_UBspline_2d_z(Ugrid x_grid, Ugrid y_grid, BCtype_z xBC, BCtype_z yBC,
+                                                 int num_splines);
+void set_multi_UBspline_1d_z(multi_UBspline_1d_z *spline, int spline_num, complex_double *data);
+void set_multi_UBspline_2d_z(multi_UBspline_2d_z *spline, int spline_num, complex_double *data);
+/* src/multi_bspline_create.h:94 and :161: one spline solved with its
+ * own x boundary condition.  The codes must be periodic (or antiperiodic)
+ * exactly when the table's are (the table size depends on it); otherwise
+ * the call fails with EINVAL (the reference would write past the table). */
+void set_multi_UBspline_1d_d_BC(multi_UBspline_1d_d *spline, int spline_num, double *data, BCtype_d xBC);
+void set_multi_UBspline_1d_z_BC(multi_UBspline_1d_z *spline, int spline_num, complex_double *data, BCtype_z xBC);
 
 /* src/multi_bspline_create.h:60-63; src/multi_bspline_create.c:252-321 */
 multi_UBspline_3d_s *

@@ -20,6 +20,20 @@
 extern "C" {
 #endif
 
+/* 1D (src/multi_bspline_create_cuda.h:10-28; the reference implements s and
+ * c, src/multi_bspline_create_cuda.cu:17-237, and declares d and z). */
+multi_UBspline_1d_s_cuda *create_multi_UBspline_1d_s_cuda(multi_UBspline_1d_s *spline);
+multi_UBspline_1d_s_cuda *create_multi_UBspline_1d_s_cuda_conv(multi_UBspline_1d_d *spline);
+multi_UBspline_1d_c_cuda *create_multi_UBspline_1d_c_cuda(multi_UBspline_1d_c *spline);
+multi_UBspline_1d_c_cuda *create_multi_UBspline_1d_c_cuda_conv(multi_UBspline_1d_z *spline);
+multi_UBspline_1d_d_cuda *create_multi_UBspline_1d_d_cuda(multi_UBspline_1d_d *spline);
+multi_UBspline_1d_z_cuda *create_multi_UBspline_1d_z_cuda(multi_UBspline_1d_z *spline);
+void destroy_multi_UBspline_1d_s_cuda(multi_UBspline_1d_s_cuda *spline);
+void destroy_multi_UBspline_1d_c_cuda(multi_UBspline_1d_c_cuda *spline);
+void destroy_multi_UBspline_1d_d_cuda(multi_UBspline_1d_d_cuda *spline);
+void destroy_multi_UBspline_1d_z_cuda(multi_UBspline_1d_z_cuda *spline);
+
+/* 3D */
 multi_UBspline_3d_s_cuda *create_multi_UBspline_3d_s_cuda(multi_UBspline_3d_s *spline);
 multi_UBspline_3d_s_cuda *create_multi_UBspline_3d_s_cuda_conv(multi_UBspline_3d_d *spline);
 multi_UBspline_3d_c_cuda *create_multi_UBspline_3d_c_cuda(multi_UBspline_3d_c *spline);

@@ -1,5 +1,5 @@
 /*
- * multi_bspline_eval_c.h -- single-point evaluation of a uniform 3D
+ * multi_bspline_eval_c.h -- single-point evaluation of a uniform 1D/2D/3D
  * multi-spline of type c (complex_float), host output buffers.
  *
  * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_c.h:92-115
@@ -20,6 +20,22 @@
 extern "C" {
 #endif
 
+/* ---- 1D and 2D (src/multi_bspline_eval_c.h:32-81; std backend
+ * src/multi_bspline_eval_std_c_impl.h).  1D: grads[N], lapl[N] and hess[N]
+ * are first and second derivatives (the 1D vgh equals the vgl, as in the
+ * reference).  2D: grads[N][2], lapl[N] = d2/dx2 + d2/dy2, hess[N][2][2]. */
+void eval_multi_UBspline_1d_c(multi_UBspline_1d_c *spline, double x, complex_float *vals);
+void eval_multi_UBspline_1d_c_vg(multi_UBspline_1d_c *spline, double x, complex_float *vals, complex_float *grads);
+void eval_multi_UBspline_1d_c_vgl(multi_UBspline_1d_c *spline, double x, complex_float *vals, complex_float *grads, complex_float *lapl);
+void eval_multi_UBspline_1d_c_vgh(multi_UBspline_1d_c *spline, double x, complex_float *vals, complex_float *grads, complex_float *hess);
+void eval_multi_UBspline_2d_c(multi_UBspline_2d_c *spline, double x, double y, complex_float *vals);
+void eval_multi_UBspline_2d_c_vg(multi_UBspline_2d_c *spline, double x, double y, complex_float *vals, complex_float *grads);
+void eval_multi_UBspline_2d_c_vgl(multi_UBspline_2d_c *spline, double x, double y, complex_float *vals, complex_float *grads,
+                                   complex_float *lapl);
+void eval_multi_UBspline_2d_c_vgh(multi_UBspline_2d_c *spline, double x, double y, complex_float *vals, complex_float *grads,
+                                   complex_float *hess);
+
+/* ---- 3D */
 void eval_multi_UBspline_3d_c(multi_UBspline_3d_c *spline, double x, double y, double z,
                                complex_float *vals);
 

@@ -1,7 +1,8 @@
 /*
  * multi_bspline_eval_cuda.h -- batched multi-point evaluation on the GPU.
  *
- * Replaces the 3D value, sign, vgh and vgl entries of src/multi_bspline_eval_cuda.h:62-137
+ * Replaces the 1D value and vgl entries and the 3D value, sign, vgh and vgl
+ * entries of src/multi_bspline_eval_cuda.h:12-137
  * (kernels and launchers in src/multi_bspline_cuda_{s,d,c,z}_impl.h).
  * Same arguments and meaning:
  *   pos_d   device array of num points, xyz interleaved (float for s/c,
@@ -27,6 +28,35 @@
 extern "C" {
 #endif
 
+/* ---- 1D (src/multi_bspline_eval_cuda.h:12-55; the reference implements s
+ * and c, src/multi_bspline_cuda_s_impl.h:10-175, src/multi_bspline_cuda_c_impl.h:9-175).
+ * pos_d holds one coordinate per point; vals_d, grads_d and lapl_d are
+ * device arrays of num device pointers, each to N reals (2N for complex,
+ * re/im interleaved).  As in the reference's kernels, the gradient and
+ * second derivative are taken with respect to the cell coordinate
+ * u = r * gridInv: they are NOT multiplied by gridInv and gridInv^2
+ * (multiply them yourself for derivatives in position units).  The
+ * reference leaves grads/lapl of the last N mod 64 columns unwritten; here
+ * every column is written. */
+void eval_multi_multi_UBspline_1d_s_cuda(multi_UBspline_1d_s_cuda *spline, float *pos_d, float *vals_d[], int num);
+void eval_multi_multi_UBspline_1d_s_vgl_cuda(multi_UBspline_1d_s_cuda *spline, float *pos_d, float *vals_d[],
+                                             float *grads_d[], float *lapl_d[], int num);
+void eval_multi_multi_UBspline_1d_d_cuda(multi_UBspline_1d_d_cuda *spline, double *pos_d, double *vals_d[],
+                                         int num);
+void eval_multi_multi_UBspline_1d_d_vgl_cuda(multi_UBspline_1d_d_cuda *spline, double *pos_d, double *vals_d[],
+                                             double *grads_d[], double *lapl_d[], int num);
+void eval_multi_multi_UBspline_1d_c_cuda(multi_UBspline_1d_c_cuda *spline, float *pos_d, complex_float *vals_d[],
+                                         int num);
+void eval_multi_multi_UBspline_1d_c_vgl_cuda(multi_UBspline_1d_c_cuda *spline, float *pos_d,
+                                             complex_float *vals_d[], complex_float *grads_d[],
+                                             complex_float *lapl_d[], int num);
+void eval_multi_multi_UBspline_1d_z_cuda(multi_UBspline_1d_z_cuda *spline, double *pos_d, complex_double *vals_d[],
+                                         int num);
+void eval_multi_multi_UBspline_1d_z_vgl_cuda(multi_UBspline_1d_z_cuda *spline, double *pos_d,
+                                             complex_double *vals_d[], complex_double *grads_d[],
+                                             complex_double *lapl_d[], int num);
+
+/* ---- 3D */
 /* src/multi_bspline_eval_cuda.h:62-64; src/multi_bspline_cuda_s_impl.h:488 */
 void eval_multi_multi_UBspline_3d_s_cuda(multi_UBspline_3d_s_cuda *spline, float *pos_d,
                                          float *vals_d[], int num);

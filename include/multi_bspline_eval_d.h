@@ -1,5 +1,5 @@
 /*
- * multi_bspline_eval_d.h -- single-point evaluation of a uniform 3D
+ * multi_bspline_eval_d.h -- single-point evaluation of a uniform 1D/2D/3D
  * multi-spline of type d (double), host output buffers.
  *
  * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_d.h:88-111
@@ -20,6 +20,22 @@
 extern "C" {
 #endif
 
+/* ---- 1D and 2D (src/multi_bspline_eval_d.h:32-78; std backend
+ * src/multi_bspline_eval_std_d_impl.h).  1D: grads[N], lapl[N] and hess[N]
+ * are first and second derivatives (the 1D vgh equals the vgl, as in the
+ * reference).  2D: grads[N][2], lapl[N] = d2/dx2 + d2/dy2, hess[N][2][2]. */
+void eval_multi_UBspline_1d_d(multi_UBspline_1d_d *spline, double x, double *vals);
+void eval_multi_UBspline_1d_d_vg(multi_UBspline_1d_d *spline, double x, double *vals, double *grads);
+void eval_multi_UBspline_1d_d_vgl(multi_UBspline_1d_d *spline, double x, double *vals, double *grads, double *lapl);
+void eval_multi_UBspline_1d_d_vgh(multi_UBspline_1d_d *spline, double x, double *vals, double *grads, double *hess);
+void eval_multi_UBspline_2d_d(multi_UBspline_2d_d *spline, double x, double y, double *vals);
+void eval_multi_UBspline_2d_d_vg(multi_UBspline_2d_d *spline, double x, double y, double *vals, double *grads);
+void eval_multi_UBspline_2d_d_vgl(multi_UBspline_2d_d *spline, double x, double y, double *vals, double *grads,
+                                   double *lapl);
+void eval_multi_UBspline_2d_d_vgh(multi_UBspline_2d_d *spline, double x, double y, double *vals, double *grads,
+                                   double *hess);
+
+/* ---- 3D */
 void eval_multi_UBspline_3d_d(multi_UBspline_3d_d *spline, double x, double y, double z,
                                double *vals);
 

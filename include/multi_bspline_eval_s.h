@@ -1,5 +1,5 @@
 /*
- * multi_bspline_eval_s.h -- single-point evaluation of a uniform 3D
+ * multi_bspline_eval_s.h -- single-point evaluation of a uniform 1D/2D/3D
  * multi-spline of type s (float), host output buffers.
  *
  * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_s.h:87-110
@@ -20,6 +20,22 @@
 extern "C" {
 #endif
 
+/* ---- 1D and 2D (src/multi_bspline_eval_s.h:30-77; std backend
+ * src/multi_bspline_eval_std_s_impl.h).  1D: grads[N], lapl[N] and hess[N]
+ * are first and second derivatives (the 1D vgh equals the vgl, as in the
+ * reference).  2D: grads[N][2], lapl[N] = d2/dx2 + d2/dy2, hess[N][2][2]. */
+void eval_multi_UBspline_1d_s(multi_UBspline_1d_s *spline, double x, float *vals);
+void eval_multi_UBspline_1d_s_vg(multi_UBspline_1d_s *spline, double x, float *vals, float *grads);
+void eval_multi_UBspline_1d_s_vgl(multi_UBspline_1d_s *spline, double x, float *vals, float *grads, float *lapl);
+void eval_multi_UBspline_1d_s_vgh(multi_UBspline_1d_s *spline, double x, float *vals, float *grads, float *hess);
+void eval_multi_UBspline_2d_s(multi_UBspline_2d_s *spline, double x, double y, float *vals);
+void eval_multi_UBspline_2d_s_vg(multi_UBspline_2d_s *spline, double x, double y, float *vals, float *grads);
+void eval_multi_UBspline_2d_s_vgl(multi_UBspline_2d_s *spline, double x, double y, float *vals, float *grads,
+                                   float *lapl);
+void eval_multi_UBspline_2d_s_vgh(multi_UBspline_2d_s *spline, double x, double y, float *vals, float *grads,
+                                   float *hess);
+
+/* ---- 3D */
 void eval_multi_UBspline_3d_s(multi_UBspline_3d_s *spline, double x, double y, double z,
                                float *vals);
 

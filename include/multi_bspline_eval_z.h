@@ -1,5 +1,5 @@
 /*
- * multi_bspline_eval_z.h -- single-point evaluation of a uniform 3D
+ * multi_bspline_eval_z.h -- single-point evaluation of a uniform 1D/2D/3D
  * multi-spline of type z (complex_double), host output buffers.
  *
  * Replaces the 3D value, vg, vgl and vgh entries of src/multi_bspline_eval_z.h:87-110
@@ -20,6 +20,22 @@
 extern "C" {
 #endif
 
+/* ---- 1D and 2D (src/multi_bspline_eval_z.h:29-77; std backend
+ * src/multi_bspline_eval_std_z_impl.h).  1D: grads[N], lapl[N] and hess[N]
+ * are first and second derivatives (the 1D vgh equals the vgl, as in the
+ * reference).  2D: grads[N][2], lapl[N] = d2/dx2 + d2/dy2, hess[N][2][2]. */
+void eval_multi_UBspline_1d_z(multi_UBspline_1d_z *spline, double x, complex_double *vals);
+void eval_multi_UBspline_1d_z_vg(multi_UBspline_1d_z *spline, double x, complex_double *vals, complex_double *grads);
+void eval_multi_UBspline_1d_z_vgl(multi_UBspline_1d_z *spline, double x, complex_double *vals, complex_double *grads, complex_double *lapl);
+void eval_multi_UBspline_1d_z_vgh(multi_UBspline_1d_z *spline, double x, complex_double *vals, complex_double *grads, complex_double *hess);
+void eval_multi_UBspline_2d_z(multi_UBspline_2d_z *spline, double x, double y, complex_double *vals);
+void eval_multi_UBspline_2d_z_vg(multi_UBspline_2d_z *spline, double x, double y, complex_double *vals, complex_double *grads);
+void eval_multi_UBspline_2d_z_vgl(multi_UBspline_2d_z *spline, double x, double y, complex_double *vals, complex_double *grads,
+                                   complex_double *lapl);
+void eval_multi_UBspline_2d_z_vgh(multi_UBspline_2d_z *spline, double x, double y, complex_double *vals, complex_double *grads,
+                                   complex_double *hess);
+
+/* ---- 3D */
 void eval_multi_UBspline_3d_z(multi_UBspline_3d_z *spline, double x, double y, double z,
                                complex_double *vals);
 
