@@ -37,6 +37,8 @@ METRIC = "vgh spline-evals/s (64³, 1024 orbitals) FP16-coef vs FP32; p50/p99 la
 UNIT = "spline-evals/s"
 BYTES_F32 = 64 * 4 + 10 * 4   # algorithmic bytes per vgh spline-eval, FP32 table
 BYTES_F16 = 64 * 2 + 10 * 4   # FP16 table (per-spline scale amortised to 0)
+KERNEL_BY_MODE = {0: "k_eval<F16,vgh>", 1: "k_eval<F16,vgh> (L2 bulk prefetch)", 2: "k_eval_pipe<F16,vgh>",
+                  3: "k_eval_pipe<F16,vgh,wide>"}
 
 
 def dist_env():
@@ -394,7 +396,7 @@ def run_gpu(args):
                        if serving else None),
         "serving": ({"sweep": serving, **serving_stats} if serving else None),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "k_eval<F16,vgh>",
+                     "peak_kind": peak_kind, "kernel": KERNEL_BY_MODE[tiles["f16"]["load_mode"]],
                      "bytes_per_eval": BYTES_F16,
                      "traffic": (tr * evals_per_launch if tr else None),
                      "fp32": {"achieved": rate32 / world * BYTES_F32 / 1e9,

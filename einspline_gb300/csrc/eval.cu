@@ -583,10 +583,14 @@ int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const 
   return 0;
 }
 
+// Untuned defaults for vgh are the autotuner's choices on GB300 at 64^3 x
+// 1024 and 128^3 x 2048: the shared-memory copy pipeline, 8-column wide for
+// 16-bit tables; FP64 (FMA-bound) and value-only evaluation use direct loads.
 int pick_mode(Table *t, bool vgh) {
   if (t->tile_mode >= 0) return t->tile_mode;
   const int v = vgh ? 1 : 0;
   if (t->tuned_tx[v]) return t->tuned_mode[v];
+  if (vgh && t->storage != ST_F64) return is16(t->storage) ? 3 : 2;
   return 0;
 }
 
@@ -597,6 +601,14 @@ void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb) {
   const int VW = elems_per_thread(t);
   const int need = (t->ncol + VW - 1) / VW;
   tx = (need + 31) / 32 * 32;
+  if (vgh && t->storage != ST_F64 && t->tile_mode < 0) {
+    // pipelined defaults (pick_mode): one lane of points, 8 points a block
+    const int cap = is16(t->storage) ? 32 : 64;
+    tx = tx > cap ? cap : tx;
+    ty = 1;
+    pb = 8;
+    return;
+  }
   if (tx > 256) tx = 256;
   ty = 256 / tx;
   if (ty > 8) ty = 8;

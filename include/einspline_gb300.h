@@ -172,7 +172,9 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  *      (FP32 and 16-bit tables; one point lane per block);
  *   3: as 2 with 8 columns and one 16-byte copy per thread and row (16-bit
  *      tables; others use 2);
- *  -1: the autotuned choice (default 0).  Results are identical in all modes. */
+ *  -1: the autotuned choice; untuned, vgh uses 3 for 16-bit tables and 2
+ *      for FP32 (the choices the autotuner makes on GB300), value-only and
+ *      FP64 use 0.  Results are identical in all modes. */
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode);
 int einspline_gb300_get_load_mode(einspline_gb300_table *t);
 /* Time every candidate tile in every load mode on this table for npts
