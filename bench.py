@@ -564,7 +564,13 @@ def other_configs(args):
     t.autotune(128 * 256)
     p = torch.from_numpy(synth.points_uniform(203, 128 * 256)).cuda()
     r = rate(t, p)
-    out["C2_d_48cube_512"] = {"evals_per_s": r, "GBps_alg": r * 592 / 1e9, "tile": list(t.get_tile())}
+    t.set_fp64_mode(1)
+    r_df = rate(t, p)
+    t.set_fp64_mode(0)
+    out["C2_d_48cube_512"] = {"evals_per_s": r, "GBps_alg": r * 592 / 1e9, "tile": list(t.get_tile()),
+                              "double_float": {"evals_per_s": r_df, "GBps_alg": r_df * 592 / 1e9,
+                                               "note": "einspline_gb300_set_fp64_mode(1): FP64 table, "
+                                                       "double-float arithmetic (tested to 1e-12 of FP64)"}}
     del t
     t = dev_table("c", 64, 256, 303)
     t.autotune(256 * 128)

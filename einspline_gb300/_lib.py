@@ -202,6 +202,8 @@ def _signatures():
     sig["einspline_gb300_eval_3d_host"] = ([vp, C.POINTER(EvalOpts), i64, vp, vp, vp, vp], i32)
     sig["einspline_gb300_eval_3d_sorted_noalloc"] = ([vp, C.POINTER(EvalOpts), i64, vp, vp, vp, vp, vp], i32)
     sig["einspline_gb300_set_host_direct"] = ([vp, i32], i32)
+    sig["einspline_gb300_set_fp64_mode"] = ([vp, i32], i32)
+    sig["einspline_gb300_get_fp64_mode"] = ([vp], i32)
     sig["einspline_gb300_set_tile"] = ([vp, i32, i32, i32], i32)
     sig["einspline_gb300_get_tile"] = ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32)
     sig["einspline_gb300_autotune"] = ([vp, i64, i32], i32)

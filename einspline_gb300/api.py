@@ -230,6 +230,11 @@ class MultiUBspline3D:
         check()
         return out
 
+    def set_fp64_mode(self, mode: int) -> None:
+        """FP64 tables: 0 IEEE FP64 evaluation, 1 double-float arithmetic."""
+        _lib().einspline_gb300_set_fp64_mode(self.table, int(mode))
+        check()
+
     def set_host_direct(self, mode: int) -> None:
         _lib().einspline_gb300_set_host_direct(self.table, int(mode))
         check()
@@ -291,6 +296,11 @@ class CudaSpline:
     @property
     def fields(self):
         return self.ptr.contents
+
+    def set_fp64_mode(self, mode: int) -> None:
+        """The handle's own table: 0 IEEE FP64, 1 double-float arithmetic."""
+        _lib().einspline_gb300_set_fp64_mode(self.table, int(mode))
+        check()
 
     def eval_multi(self, pos, vgh=True, outs=None):
         """eval_multi_multi_UBspline_3d_*[_vgh]_cuda with per-point output

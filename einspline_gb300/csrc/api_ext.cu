@@ -159,6 +159,31 @@ static void *mapped_address(const void *h) {
   return (at.type == cudaMemoryTypeHost && at.devicePointer) ? at.devicePointer : nullptr;
 }
 
+int einspline_gb300_set_fp64_mode(einspline_gb300_table *t, int mode) {
+  clear();
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle (3D tables only)");
+  if (mode != 0 && mode != 1) return fail(EINSPLINE_GB300_EINVAL, "mode must be 0 or 1");
+  if (t->storage != ST_F64) return mode ? fail(EINSPLINE_GB300_EINVAL, "not an FP64 (d/z) table") : 0;
+  if (int r = table_flush(t)) return r;
+  {
+    std::lock_guard<std::mutex> lock(t->mu);
+    t->fp64_mode = mode;
+    t->df_stale = true;
+    if (mode == 0) {
+      cudaFree(t->df_coefs);  // synchronises the device: no launch still reads it
+      t->df_coefs = nullptr;
+      return 0;
+    }
+  }
+  return table_df_refresh(t);
+}
+
+int einspline_gb300_get_fp64_mode(einspline_gb300_table *t) {
+  clear();
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle (3D tables only)");
+  return t->fp64_mode;
+}
+
 int einspline_gb300_set_host_direct(einspline_gb300_table *t, int mode) {
   clear();
   if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");

@@ -14,7 +14,9 @@ namespace eg {
 
 constexpr uint32_t kMagic = 0x45473330u;  // "EG30"
 
-enum Storage { ST_NATIVE = 0, ST_F32 = 1, ST_F16 = 2, ST_BF16 = 3, ST_F64 = 4, ST_I16 = 5 };
+enum Storage { ST_NATIVE = 0, ST_F32 = 1, ST_F16 = 2, ST_BF16 = 3, ST_F64 = 4, ST_I16 = 5,
+               // kernel-only: an FP64 table read from its double-float shadow
+               ST_DF = 6 };
 __host__ __device__ constexpr bool is16(int st) { return st == ST_F16 || st == ST_BF16 || st == ST_I16; }
 // I16 values are stored with this bias so that a 16-bit pattern u becomes
 // the float 2^23 + u by inserting it under the exponent of 2^23.
@@ -85,6 +87,11 @@ struct einspline_gb300_table {
   size_t table_bytes = 0;
   void *coefs = nullptr;            // device
   float *scale = nullptr;           // device, ncol_pad floats (16-bit storage)
+  // FP64 tables: 0 evaluate in IEEE FP64; 1 in double-float arithmetic from
+  // a shadow copy holding each coefficient as (hi, lo) floats
+  int fp64_mode = 0;
+  void *df_coefs = nullptr;         // device, table_bytes
+  bool df_stale = true;
   bool owns = true;
 
   // queued set calls
@@ -150,6 +157,9 @@ int table_set(Table *t, int first, int count, const void *data, bool from_device
 int table_set_bc(Table *t, int spline, const void *data, int lcode, int rcode, const double lval[2],
                  const double rval[2]);
 int table_flush(Table *t);
+// Rebuilds the double-float shadow of an FP64 table when fp64_mode is 1 and
+// the table changed since it was made.
+int table_df_refresh(Table *t);
 inline bool table_ok(const Table *t) { return t && t->magic == kMagic; }
 // A 3D table: what every 3D entry point and extension takes.
 inline bool table3_ok(const Table *t) { return table_ok(t) && t->dims == 3; }

@@ -206,9 +206,18 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
     else if (a.pos_f64) xd = reinterpret_cast<const double *>(a.pos)[3 * src + ax];
     else xd = (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
     int idx;
-    A t;
-    cell(a, ax, xd, idx, t);
-    bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
+    if constexpr (ST == ST_DF) {
+      // FP64 cell and weights, carried into the reduction as hi + lo
+      double t, w[12];
+      cell(a, ax, xd, idx, t);
+      bspline_weights<double>(t, w, a.dinv[ax]);
+#pragma unroll
+      for (int m = 0; m < 12; m++) sw[pp * 36 + ax * 12 + m] = to_dfl(w[m]);
+    } else {
+      A t;
+      cell(a, ax, xd, idx, t);
+      bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
+    }
     sidx[pp * 3 + ax] = idx;
     if (ax == 0) ssrc[pp] = src;
   }
@@ -239,7 +248,16 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
     const char *base = cbase + sidx[3 * pp] * xsb + sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
     A o[10][VW];
     contract<ST, VGH>(base, xsb, ysb, zsb, sw + pp * 36, o);
-    epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
+    if constexpr (ST == ST_DF) {
+      double od[10][VW];
+#pragma unroll
+      for (int q = 0; q < (VGH ? 10 : 1); q++)
+#pragma unroll
+        for (int e = 0; e < VW; e++) od[q][e] = to_double(o[q][e]);
+      epilogue<double, VW, VGH>(a, ssrc[pp], col0, od);
+    } else {
+      epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
+    }
   }
 }
 
@@ -495,19 +513,37 @@ void fill_eval_geometry(const Table *t, EvalArgs &a) {
 
 // Load modes: 0 direct, 1 L2 prefetch + direct, 2 shared-memory pipeline,
 // 3 shared-memory pipeline with 8 columns per thread (16-bit tables).
+// (The double-float path has only the direct-load kernel: FP64 tables never
+// take the pipelined modes.)
 template <int ST, bool VGH>
 static const void *kernel_for(int mode) {
-  if (mode == 2) return (const void *)k_eval_pipe<ST, VGH, false>;
-  if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
+  if constexpr (ST != ST_DF) {
+    if (mode == 2) return (const void *)k_eval_pipe<ST, VGH, false>;
+    if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
+  }
   return (const void *)k_eval<ST, VGH>;
 }
 
 template <int ST, bool VGH>
 static cudaError_t launch_k(const EvalArgs &a, unsigned grid, dim3 block, size_t smem, cudaStream_t s) {
-  if (a.mode == 2) k_eval_pipe<ST, VGH, false><<<grid, block, smem, s>>>(a);
-  else if (a.mode == 3) k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)><<<grid, block, smem, s>>>(a);
-  else k_eval<ST, VGH><<<grid, block, smem, s>>>(a);
+  if constexpr (ST != ST_DF) {
+    if (a.mode == 2) {
+      k_eval_pipe<ST, VGH, false><<<grid, block, smem, s>>>(a);
+      return cudaGetLastError();
+    }
+    if (a.mode == 3) {
+      k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)><<<grid, block, smem, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
+  k_eval<ST, VGH><<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+// The kernel type of a table's launches: its storage, or the double-float
+// shadow of an FP64 table in fp64_mode 1.
+static int kernel_storage(const Table *t) {
+  return (t->storage == ST_F64 && t->fp64_mode == 1 && t->df_coefs) ? (int)ST_DF : t->storage;
 }
 
 // Kernel, block and dynamic shared memory of a launch; the pipelined kernel
@@ -534,7 +570,10 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
     *smem = align_up(*smem, 16) + pipe_bytes(tx, rb);
   }
   *block = dim3(tx, ty);
-  switch (t->storage) {
+  const int ks = kernel_storage(t);
+  if (ks == ST_DF) a.coefs = t->df_coefs;
+  switch (ks) {
+    case ST_DF: *func = vgh ? kernel_for<ST_DF, true>(a.mode) : kernel_for<ST_DF, false>(a.mode); break;
     case ST_F32: *func = vgh ? kernel_for<ST_F32, true>(a.mode) : kernel_for<ST_F32, false>(a.mode); break;
     case ST_F16: *func = vgh ? kernel_for<ST_F16, true>(a.mode) : kernel_for<ST_F16, false>(a.mode); break;
     case ST_BF16: *func = vgh ? kernel_for<ST_BF16, true>(a.mode) : kernel_for<ST_BF16, false>(a.mode); break;
@@ -557,7 +596,9 @@ int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty,
   const int64_t blocks = ((a.npts + pb - 1) / pb) * a.ntiles;
   if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
   cudaError_t e;
-  switch (t->storage) {
+  switch (kernel_storage(t)) {
+    case ST_DF: e = vgh ? launch_k<ST_DF, true>(a, (unsigned)blocks, block, smem, s)
+                        : launch_k<ST_DF, false>(a, (unsigned)blocks, block, smem, s); break;
     case ST_F32: e = vgh ? launch_k<ST_F32, true>(a, (unsigned)blocks, block, smem, s)
                          : launch_k<ST_F32, false>(a, (unsigned)blocks, block, smem, s); break;
     case ST_F16: e = vgh ? launch_k<ST_F16, true>(a, (unsigned)blocks, block, smem, s)

@@ -9,6 +9,46 @@
 
 namespace eg {
 
+// ------------------------------------------------------------ double-float
+// A value carried as an unevaluated sum h + l of two floats (about 48
+// significant bits).  Products use the exact FMA residual of h*h' plus the
+// cross terms; sums use Knuth's two-sum (Knuth, TAOCP vol. 2, 4.2.2;
+// Dekker 1971), then a fast renormalisation.  Only round-to-nearest
+// intrinsics are used, so no contraction can change the error terms.  For
+// the FP64 tables on GB300, whose FP64 pipe is a small fraction of the FP32
+// one: 15 FP32 operations per multiply-add instead of one DFMA.
+struct dfl {
+  float h, l;
+  __host__ __device__ dfl() {}
+  __host__ __device__ constexpr dfl(float x) : h(x), l(0.f) {}
+  __host__ __device__ constexpr dfl(float a, float b) : h(a), l(b) {}
+};
+
+__device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return dfl(p, e);
+}
+
+// c + a * b
+__device__ __forceinline__ dfl fmaT(dfl a, dfl b, dfl c) {
+  const dfl p = a * b;
+  const float s = __fadd_rn(c.h, p.h);
+  const float bb = __fsub_rn(s, c.h);
+  float t = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p.h, bb));
+  t = __fadd_rn(t, __fadd_rn(c.l, p.l));
+  const float hs = __fadd_rn(s, t);
+  return dfl(hs, __fsub_rn(t, __fsub_rn(hs, s)));
+}
+
+__device__ __forceinline__ dfl to_dfl(double x) {
+  const float h = __double2float_rn(x);
+  return dfl(h, __double2float_rn(__dsub_rn(x, (double)h)));
+}
+__device__ __forceinline__ double to_double(dfl x) { return __dadd_rn((double)x.h, (double)x.l); }
+
 // ------------------------------------------------------------ coefficient types
 // Raw is what one thread reads per stencil row (VW stored reals); decode
 // turns it into VW accumulator values.
@@ -59,6 +99,18 @@ template <> struct CT<ST_F64> {
   using Raw = double2;
   static constexpr int VW = 2, BYTES = 8;
   __device__ static __forceinline__ void decode(const Raw &x, double (&v)[2]) { v[0] = x.x; v[1] = x.y; }
+};
+
+// The double-float shadow of an FP64 table: (hi, lo) per coefficient, two
+// columns per 16-byte load.
+template <> struct CT<ST_DF> {
+  using A = dfl;
+  using Raw = float4;
+  static constexpr int VW = 2, BYTES = 8;
+  __device__ static __forceinline__ void decode(const Raw &x, dfl (&v)[2]) {
+    v[0] = dfl(x.x, x.y);
+    v[1] = dfl(x.z, x.w);
+  }
 };
 
 template <int ST>

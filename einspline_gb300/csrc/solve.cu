@@ -495,6 +495,7 @@ void table_destroy(Table *t) {
   free_work(t);
   if (t->owns) cudaFree(t->coefs);
   cudaFree(t->scale);
+  cudaFree(t->df_coefs);
   cudaFree(t->factors_d);
   cudaFree(t->pt_dev);
   if (t->pt_host) cudaFreeHost(t->pt_host);
@@ -620,13 +621,48 @@ static int flush_locked(Table *t, const AxisOverride *ov = nullptr) {
   return 0;
 }
 
+// Each FP64 coefficient as (hi, lo) = (round(c), round(c - hi)).
+__global__ void k_to_df(const double *__restrict__ c, float2 *__restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = c[i];
+    const float h = __double2float_rn(v);
+    out[i] = make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+  }
+}
+
+static int df_refresh_locked(Table *t) {
+  if (t->fp64_mode != 1 || t->storage != ST_F64 || !t->df_stale) return 0;
+  if (!t->df_coefs && cudaMalloc(&t->df_coefs, t->table_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    t->df_coefs = nullptr;
+    return fail(EINSPLINE_GB300_ENOMEM, "cannot allocate the double-float copy of the table (%zu bytes)",
+                t->table_bytes);
+  }
+  const int64_t n = (int64_t)(t->table_bytes / sizeof(double));
+  k_to_df<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, t->stream>>>((const double *)t->coefs,
+                                                                                      (float2 *)t->df_coefs, n);
+  count_launch();
+  EG_CUDA(cudaGetLastError());
+  EG_CUDA(cudaStreamSynchronize(t->stream));
+  t->df_stale = false;
+  return 0;
+}
+
+int table_df_refresh(Table *t) {
+  std::lock_guard<std::mutex> g(t->mu);
+  return df_refresh_locked(t);
+}
+
 int table_flush(Table *t) {
   std::lock_guard<std::mutex> g(t->mu);
   const bool had = !t->pend_spline.empty();
   if (int r = flush_locked(t)) return r;
   // Evaluations may run on any stream: make the solved table visible to all.
-  if (had) EG_CUDA(cudaStreamSynchronize(t->stream));
-  return 0;
+  if (had) {
+    EG_CUDA(cudaStreamSynchronize(t->stream));
+    t->df_stale = true;
+  }
+  return df_refresh_locked(t);
 }
 
 int table_set_bc(Table *t, int spline, const void *data, int lcode, int rcode, const double lval[2],

@@ -288,6 +288,22 @@ int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_de
 int einspline_gb300_det_update(const einspline_gb300_det_opts *opts, int naccept, float *const *a_d,
                                float *const *ainv_d, const float *const *row_d, float *work_d, void *stream);
 
+/* FP64 (d and z) tables: how evaluations compute.
+ *   0 (default): IEEE FP64 fused multiply-adds.  On GB300 the FP64 pipe is a
+ *     small fraction of the FP32 one, and this path is bound by it, far below
+ *     the memory roofline.
+ *   1: double-float arithmetic on the FP32 pipes: each coefficient and basis
+ *     weight as an unevaluated sum of two floats (hi + lo, ~48 significant
+ *     bits), error-free products by FMA residuals and two-sum accumulation;
+ *     results within ~1e-14 relative of FP64 (tested to 1e-12 against the
+ *     FP64 oracle).  Keeps a (hi, lo) copy of the table in device memory (the
+ *     table's size again), rebuilt after set_* / flush.
+ * Applies to every 3D evaluation of the table (flat, host-buffer, server,
+ * single-point and *_cuda entries of a handle made from it take the handle's
+ * own table: set the mode on c->gb300).  Not for 1D/2D tables. */
+int einspline_gb300_set_fp64_mode(einspline_gb300_table *t, int mode);
+int einspline_gb300_get_fp64_mode(einspline_gb300_table *t);
+
 /* Kernel launches (and graph launches) this library has issued so far. */
 int64_t einspline_gb300_launch_count(void);
 
