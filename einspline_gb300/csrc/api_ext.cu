@@ -169,6 +169,8 @@ int einspline_gb300_set_fp64_mode(einspline_gb300_table *t, int mode) {
     std::lock_guard<std::mutex> lock(t->mu);
     t->fp64_mode = mode;
     t->df_stale = true;
+    // the kernels differ between the modes: forget the tuned launch shapes
+    for (int v = 0; v < 2; v++) t->tuned_tx[v] = t->tuned_ty[v] = t->tuned_pb[v] = t->tuned_mode[v] = 0;
     if (mode == 0) {
       cudaFree(t->df_coefs);  // synchronises the device: no launch still reads it
       t->df_coefs = nullptr;

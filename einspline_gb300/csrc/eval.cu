@@ -275,6 +275,7 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   using Raw = typename CT<ST>::Raw;
   constexpr int VW = WIDE ? 2 * CT<ST>::VW : CT<ST>::VW;
   constexpr int RB = WIDE ? 2 * (int)sizeof(Raw) : (int)sizeof(Raw);
+  constexpr int NS = PipeStages<ST>::value;
   extern __shared__ __align__(16) unsigned char smem[];
   const int tile = blockIdx.x % a.ntiles;
   const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
@@ -299,12 +300,12 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   auto issue = [&](int st) {
     const int pp = st >> 2, i = st & 3;
     const char *plane = cbase + (sidx[3 * pp] + i) * xsb + sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
-    const unsigned dst = my + (unsigned)(st % kPipeStages) * slot_step;
+    const unsigned dst = my + (unsigned)(st % NS) * slot_step;
 #pragma unroll
     for (int r = 0; r < 16; r++) cp_async<RB>(dst + r * row_step, plane + (r >> 2) * ysb + (r & 3) * zsb);
   };
 #pragma unroll
-  for (int st = 0; st < kPipeStages - 1; st++) {
+  for (int st = 0; st < NS - 1; st++) {
     if (st < S) issue(st);
     cp_async_commit();
   }
@@ -312,13 +313,13 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   zero_out<A, VW>(o);
   A wz[3][4];
   for (int st = 0; st < S; st++) {
-    if (st + kPipeStages - 1 < S) issue(st + kPipeStages - 1);
+    if (st + NS - 1 < S) issue(st + NS - 1);
     cp_async_commit();
-    cp_async_wait<kPipeStages - 1>();
+    cp_async_wait<NS - 1>();
     const int pp = st >> 2, i = st & 3;
     const A *w = sw + pp * 36;
     if (i == 0) z_weights<A>(w, wz);
-    const unsigned char *slot = pipe + (size_t)(st % kPipeStages) * slot_step + (size_t)threadIdx.x * RB;
+    const unsigned char *slot = pipe + (size_t)(st % NS) * slot_step + (size_t)threadIdx.x * RB;
     reduce_plane<A, VW, VGH>(
         i, w, wz,
         [&](int j, int k, A(&c)[VW]) {
@@ -335,7 +336,16 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
         },
         o);
     if (i == 3) {
-      epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
+      if constexpr (ST == ST_DF) {
+        double od[10][VW];
+#pragma unroll
+        for (int q = 0; q < (VGH ? 10 : 1); q++)
+#pragma unroll
+          for (int e = 0; e < VW; e++) od[q][e] = to_double(o[q][e]);
+        epilogue<double, VW, VGH>(a, ssrc[pp], col0, od);
+      } else {
+        epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
+      }
       zero_out<A, VW>(o);
     }
   }
@@ -513,31 +523,23 @@ void fill_eval_geometry(const Table *t, EvalArgs &a) {
 
 // Load modes: 0 direct, 1 L2 prefetch + direct, 2 shared-memory pipeline,
 // 3 shared-memory pipeline with 8 columns per thread (16-bit tables).
-// (The double-float path has only the direct-load kernel: FP64 tables never
-// take the pipelined modes.)
+// (IEEE FP64 has only the direct-load kernel; the double-float path has the
+// direct and the 4-column pipelined kernels.)
 template <int ST, bool VGH>
 static const void *kernel_for(int mode) {
-  if constexpr (ST != ST_DF) {
-    if (mode == 2) return (const void *)k_eval_pipe<ST, VGH, false>;
-    if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
+  if constexpr (ST != ST_F64) {
+    if (mode == 2 || (mode == 3 && ST == ST_DF)) return (const void *)k_eval_pipe<ST, VGH, false>;
+    if constexpr (ST != ST_DF)
+      if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
   }
   return (const void *)k_eval<ST, VGH>;
 }
 
 template <int ST, bool VGH>
 static cudaError_t launch_k(const EvalArgs &a, unsigned grid, dim3 block, size_t smem, cudaStream_t s) {
-  if constexpr (ST != ST_DF) {
-    if (a.mode == 2) {
-      k_eval_pipe<ST, VGH, false><<<grid, block, smem, s>>>(a);
-      return cudaGetLastError();
-    }
-    if (a.mode == 3) {
-      k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)><<<grid, block, smem, s>>>(a);
-      return cudaGetLastError();
-    }
-  }
-  k_eval<ST, VGH><<<grid, block, smem, s>>>(a);
-  return cudaGetLastError();
+  const void *f = kernel_for<ST, VGH>(a.mode);
+  void *args[] = {const_cast<EvalArgs *>(&a)};
+  return cudaLaunchKernel(f, dim3(grid), block, args, smem, s);
 }
 
 // The kernel type of a table's launches: its storage, or the double-float
@@ -555,8 +557,9 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
     return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
   a.pb = pb;
   a.mode = pick_mode(t, vgh);
-  if (a.mode >= 2 && t->storage == ST_F64) a.mode = 0;  // FP64 is FMA-bound: no pipeline variant
-  if (a.mode == 3 && !is16(t->storage)) a.mode = 2;     // the wide variant is for 16-bit tables
+  const int ks = kernel_storage(t);
+  if (a.mode >= 2 && ks == ST_F64) a.mode = 0;        // IEEE FP64 is FMA-bound: no pipeline variant
+  if (a.mode == 3 && !is16(t->storage)) a.mode = 2;   // the wide variant is for 16-bit tables
   const int VW = elems_per_thread(t) * (a.mode == 3 ? 2 : 1);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   *smem = smem_total(pb, acc_bytes(t));
@@ -566,11 +569,10 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   }
   if (a.mode >= 2) {
     ty = 1;
-    const int rb = (t->storage == ST_F32 || a.mode == 3) ? 16 : 8;
-    *smem = align_up(*smem, 16) + pipe_bytes(tx, rb);
+    const int rb = (ks == ST_F32 || ks == ST_DF || a.mode == 3) ? 16 : 8;
+    *smem = align_up(*smem, 16) + pipe_bytes(tx, rb, ks == ST_DF ? PipeStages<ST_DF>::value : kPipeStages);
   }
   *block = dim3(tx, ty);
-  const int ks = kernel_storage(t);
   if (ks == ST_DF) a.coefs = t->df_coefs;
   switch (ks) {
     case ST_DF: *func = vgh ? kernel_for<ST_DF, true>(a.mode) : kernel_for<ST_DF, false>(a.mode); break;
@@ -625,13 +627,14 @@ int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const 
 }
 
 // Untuned defaults for vgh are the autotuner's choices on GB300 at 64^3 x
-// 1024 and 128^3 x 2048: the shared-memory copy pipeline, 8-column wide for
-// 16-bit tables; FP64 (FMA-bound) and value-only evaluation use direct loads.
+// 1024 and 128^3 x 2048 (and 48^3 x 512 double-float): the shared-memory
+// copy pipeline, 8-column wide for 16-bit tables; IEEE FP64 (FMA-bound) and
+// value-only evaluation use direct loads.
 int pick_mode(Table *t, bool vgh) {
   if (t->tile_mode >= 0) return t->tile_mode;
   const int v = vgh ? 1 : 0;
   if (t->tuned_tx[v]) return t->tuned_mode[v];
-  if (vgh && t->storage != ST_F64) return is16(t->storage) ? 3 : 2;
+  if (vgh && kernel_storage(t) != ST_F64) return is16(t->storage) ? 3 : 2;
   return 0;
 }
 
@@ -642,9 +645,9 @@ void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb) {
   const int VW = elems_per_thread(t);
   const int need = (t->ncol + VW - 1) / VW;
   tx = (need + 31) / 32 * 32;
-  if (vgh && t->storage != ST_F64 && t->tile_mode < 0) {
+  if (vgh && kernel_storage(t) != ST_F64 && t->tile_mode < 0) {
     // pipelined defaults (pick_mode): one lane of points, 8 points a block
-    const int cap = is16(t->storage) ? 32 : 64;
+    const int cap = is16(t->storage) ? 32 : (kernel_storage(t) == ST_DF ? 128 : 64);
     tx = tx > cap ? cap : tx;
     ty = 1;
     pb = 8;

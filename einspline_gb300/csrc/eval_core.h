@@ -5,6 +5,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "eg_internal.h"
 
 namespace eg {
@@ -13,10 +15,14 @@ namespace eg {
 // A value carried as an unevaluated sum h + l of two floats (about 48
 // significant bits).  Products use the exact FMA residual of h*h' plus the
 // cross terms; sums use Knuth's two-sum (Knuth, TAOCP vol. 2, 4.2.2;
-// Dekker 1971), then a fast renormalisation.  Only round-to-nearest
-// intrinsics are used, so no contraction can change the error terms.  For
-// the FP64 tables on GB300, whose FP64 pipe is a small fraction of the FP32
-// one: 15 FP32 operations per multiply-add instead of one DFMA.
+// Dekker 1971) on the high parts and collect every rounding error in l.
+// The pair is not renormalised after each step: a stencil sum has at most
+// 16 terms per stage, so l stays within a few ulps of h and carries its
+// errors with 24 bits to spare; the conversion to double at the end adds
+// the two parts.  Only round-to-nearest intrinsics are used, so no
+// contraction can change the error terms.  For the FP64 tables on GB300,
+// whose FP64 pipe is a small fraction of the FP32 one: 12 FP32 operations
+// per multiply-add instead of one DFMA.
 struct dfl {
   float h, l;
   __host__ __device__ dfl() {}
@@ -37,10 +43,8 @@ __device__ __forceinline__ dfl fmaT(dfl a, dfl b, dfl c) {
   const dfl p = a * b;
   const float s = __fadd_rn(c.h, p.h);
   const float bb = __fsub_rn(s, c.h);
-  float t = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p.h, bb));
-  t = __fadd_rn(t, __fadd_rn(c.l, p.l));
-  const float hs = __fadd_rn(s, t);
-  return dfl(hs, __fsub_rn(t, __fsub_rn(hs, s)));
+  const float t = __fadd_rn(__fsub_rn(c.h, __fsub_rn(s, bb)), __fsub_rn(p.h, bb));
+  return dfl(s, __fadd_rn(t, __fadd_rn(c.l, p.l)));
 }
 
 __device__ __forceinline__ dfl to_dfl(double x) {
@@ -314,9 +318,18 @@ __device__ __forceinline__ int eval_prologue(const EvalArgs &a, unsigned char *s
     else if (a.pos_f64) xd = reinterpret_cast<const double *>(a.pos)[3 * src + ax];
     else xd = (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
     int idx;
-    A t;
-    cell(a, ax, xd, idx, t);
-    bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
+    if constexpr (sizeof(A) == 8 && !std::is_same<A, double>::value) {
+      // double-float: FP64 cell and weights carried as hi + lo
+      double t, w[12];
+      cell(a, ax, xd, idx, t);
+      bspline_weights<double>(t, w, a.dinv[ax]);
+#pragma unroll
+      for (int m = 0; m < 12; m++) sw[pp * 36 + ax * 12 + m] = to_dfl(w[m]);
+    } else {
+      A t;
+      cell(a, ax, xd, idx, t);
+      bspline_weights<A>(t, sw + pp * 36 + ax * 12, sizeof(A) == 4 ? (A)a.dinvf[ax] : (A)a.dinv[ax]);
+    }
     sidx[pp * 3 + ax] = idx;
     if (ax == 0) ssrc[pp] = src;
   }
@@ -337,6 +350,15 @@ template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 constexpr int kPipeStages = 3;
-__host__ __device__ __forceinline__ size_t pipe_bytes(int nthr, int rb) { return (size_t)kPipeStages * 16 * nthr * rb; }
+__host__ __device__ __forceinline__ size_t pipe_bytes(int nthr, int rb, int stages = kPipeStages) {
+  return (size_t)stages * 16 * nthr * rb;
+}
+// Stages of the evaluation copy pipeline per kernel type: the double-float
+// reduction spends long enough on each stage that one stage in flight hides
+// the loads, and the smaller buffers let more warps share an SM.
+template <int ST>
+struct PipeStages { static constexpr int value = kPipeStages; };
+template <>
+struct PipeStages<ST_DF> { static constexpr int value = 2; };
 
 }  // namespace eg

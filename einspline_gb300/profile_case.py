@@ -19,7 +19,8 @@ import numpy as np
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16", "i16"])
+    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16", "i16", "f64"])
+    ap.add_argument("--fp64-mode", type=int, default=0, help="f64 tables: 1 evaluates in double-float arithmetic")
     ap.add_argument("--launches", type=int, default=3)
     ap.add_argument("--grid", type=int, default=64)
     ap.add_argument("--splines", type=int, default=1024)
@@ -36,17 +37,21 @@ def main():
 
     import torch
     from einspline_gb300 import api, synth
-    st = {"f32": api.STORE_F32, "f16": api.STORE_F16, "bf16": api.STORE_BF16, "i16": api.STORE_I16}[args.storage]
+    st = {"f32": api.STORE_F32, "f16": api.STORE_F16, "bf16": api.STORE_BF16, "i16": api.STORE_I16,
+          "f64": api.STORE_NATIVE}[args.storage]
+    kind = "d" if args.storage == "f64" else "s"
     g = args.grid
-    T = api.MultiUBspline3D("s", [(0.0, 1.0, g)] * 3, [(api.PERIODIC, api.PERIODIC)] * 3, args.splines,
+    T = api.MultiUBspline3D(kind, [(0.0, 1.0, g)] * 3, [(api.PERIODIC, api.PERIODIC)] * 3, args.splines,
                             storage=st)
-    buf = torch.empty((128, g, g, g), dtype=torch.float32, device="cuda")
+    buf = torch.empty((128, g, g, g), dtype=torch.float64 if kind == "d" else torch.float32, device="cuda")
     for f in range(0, args.splines, 128):
         n = min(128, args.splines - f)
         api.fill_uniform(buf[:n], 20261203, -1.0, 1.0, offset=f * g ** 3)
         T.set_device(f, buf[:n])
     T.flush()
     del buf
+    if kind == "d":
+        T.set_fp64_mode(args.fp64_mode)
     if args.det:
         # The ratio reads only row k of each transposed inverse: with k = 0 a
         # [W][1][N] buffer (row 0 of every walker's N x N matrix) is all the
@@ -76,8 +81,10 @@ def main():
     sizes = synth.walker_sizes(777, args.walkers)
     pos = torch.from_numpy(synth.points_uniform(778, int(sizes.sum()))).cuda()
     P = pos.shape[0]
-    out = (torch.empty((P, args.splines), device="cuda"), torch.empty((P, args.splines, 3), device="cuda"),
-           torch.empty((P, args.splines, 6), device="cuda"))
+    odt = torch.float64 if kind == "d" else torch.float32
+    out = (torch.empty((P, args.splines), dtype=odt, device="cuda"),
+           torch.empty((P, args.splines, 3), dtype=odt, device="cuda"),
+           torch.empty((P, args.splines, 6), dtype=odt, device="cuda"))
     torch.cuda.synchronize()
     if args.sweep:
         res = []
@@ -110,7 +117,10 @@ def main():
         e1.record()
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
-    bpe = 64 * (4 if st == api.STORE_F32 else 2) + (40 if args.vgh else 4)
+    if kind == "d":
+        bpe = 64 * 8 + (80 if args.vgh else 8)
+    else:
+        bpe = 64 * (4 if st == api.STORE_F32 else 2) + (40 if args.vgh else 4)
     print(json.dumps({"storage": args.storage, "points": P, "splines": args.splines, "ms": times,
                       "tile": T.get_tile(), "bytes_per_eval": bpe,
                       "GBps": [P * args.splines * bpe / (t * 1e-3) / 1e9 for t in times]}))
