@@ -526,6 +526,47 @@ def det_step(tabs, W=2048, reps=20):
     return out
 
 
+def lowdim_1d(P=262144, reps=10):
+    """1D multi-spline (periodic, 512 points, 1024 real float splines): the
+    batched GPU vgl entry eval_multi_multi_UBspline_1d_s_vgl_cuda against the
+    reference's CPU 1D vgl (the oracle port, OpenMP over points, all cores)
+    on a bounded sample.  Algorithmic bytes per eval: 4 coefficients + 3
+    outputs = 28 B."""
+    import torch
+    from einspline_gb300 import api, synth
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    M, N = 512, 1024
+    G = api.MultiUBsplineLD("s", [(0.0, 1.0, M)], [(api.PERIODIC, api.PERIODIC)], N)
+    data = synth.grid_data_uniform(606, (M,), N, np.float32)
+    for i in range(N):
+        G.set(i, data[i])
+    G.flush()
+    Cs = G.to_cuda()
+    pos = torch.from_numpy(synth.points_uniform(607, P, [0.0], [1.0])[:, 0].astype(np.float32)).cuda()
+    Cs.eval_multi(pos, vgl=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        Cs.eval_multi(pos, vgl=True)
+    e1.record()
+    torch.cuda.synchronize()
+    gpu = P * N * reps / (e0.elapsed_time(e1) / 1e3)
+    orc.build()
+    T = orc.Table("s", [(0.0, 1.0, M)], [(orc.PERIODIC, orc.PERIODIC)], N)
+    tab = np.ascontiguousarray(G.table_values().astype(np.float32))
+    cpos = synth.points_uniform(608, 16384, [0.0], [1.0])
+    t0 = time.perf_counter()
+    T.eval_ld_batch(cpos, 2, coefs=tab, fast=True)
+    cpu = cpos.shape[0] * N / (time.perf_counter() - t0)
+    Cs.destroy()
+    G.destroy()
+    return {"gpu_evals_per_s": gpu, "gpu_GBps_alg": gpu * 28 / 1e9, "cpu_evals_per_s": cpu,
+            "cpu_cores": orc.lib(True).orc_max_threads(), "cpu_sample": "16384 points x 1024 splines vgl",
+            "note": "one launch of 262,144 points; each call synchronises as the reference's does"}
+
+
 def other_configs(args):
     """Throughput of the other workloads (parity-test configurations, not
     the headline): C2 FP64 48^3 x 512 plane waves, 128 x 256 points; C3
@@ -578,6 +619,7 @@ def other_configs(args):
     out["C3_c_64cube_256"] = {"random_evals_per_s": rate(t, p), "sorted_evals_per_s": rate(t, p, sort=True),
                               "GBps_alg_random": rate(t, p) * 592 / 1e9}
     del t
+    out["ld1_s_512_1024"] = lowdim_1d()
     for name, st, bpe in (("f32", api.STORE_F32, 296), ("f16", api.STORE_F16, 168)):
         t = dev_table("s", 128, 2048, 505, storage=st)
         t.autotune(16384)

@@ -706,6 +706,49 @@ int orc_eval_batch(int type, int sem, int vgh, const orc_desc *d, const void *co
   return 0;
 }
 
+/* 1D/2D multi-splines at many points, OpenMP over points, outputs
+ * point-major in the CPU layouts of orc_eval_ld_* (per point: vals NC*N,
+ * grads dims*NC*N, lh NC*N or 4*NC*N for the 2D Hessian).  pos holds dims
+ * coordinates per point.  Each thread has its own 2D-laplacian scratch. */
+int orc_eval_ld_batch(int type, int dims, int form, const orc_desc *d, const void *coefs, int64_t npts,
+                      const double *pos, void *vals, void *grads, void *lh, int nthreads)
+{
+  const int64_t N = d->num_splines;
+  const int nc = (type == 'c' || type == 'z') ? 2 : 1;
+  const int rb = (type == 's' || type == 'c') ? 4 : 8;
+  const int64_t vs = nc * N, gs = dims * nc * N, hs = (dims == 2 && form == 3 ? 4 : 1) * nc * N;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+#endif
+  {
+    char *l2 = (char *)malloc((size_t)(2 * nc * N + nc) * rb);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (int64_t p = 0; p < npts; p++) {
+      const double x = pos[dims * p], y = dims == 2 ? pos[dims * p + 1] : 0.0;
+      char *v = (char *)vals + p * vs * rb;
+      char *g = form >= 1 ? (char *)grads + p * gs * rb : NULL;
+      char *h = form >= 2 ? (char *)lh + p * hs * rb : NULL;
+      switch (type) {
+        case 's': orc_eval_ld_s(d, dims, form, (const float *)coefs, x, y, (float *)v, (float *)g, (float *)h,
+                                (float *)l2); break;
+        case 'c': orc_eval_ld_c(d, dims, form, (const float *)coefs, x, y, (float *)v, (float *)g, (float *)h,
+                                (float *)l2); break;
+        case 'd': orc_eval_ld_d(d, dims, form, (const double *)coefs, x, y, (double *)v, (double *)g,
+                                (double *)h, (double *)l2); break;
+        case 'z': orc_eval_ld_z(d, dims, form, (const double *)coefs, x, y, (double *)v, (double *)g,
+                                (double *)h, (double *)l2); break;
+        default: break;
+      }
+    }
+    free(l2);
+  }
+  (void)nthreads;
+  return 0;
+}
+
 /* Number of OpenMP threads the batch entry would use (1 without OpenMP). */
 int orc_max_threads(void)
 {

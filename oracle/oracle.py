@@ -72,6 +72,9 @@ def lib(fast: bool = False) -> C.CDLL:
         L.orc_eval_batch.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(OrcDesc), C.c_void_p,
                                      C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_eval_batch.restype = C.c_int
+        L.orc_eval_ld_batch.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(OrcDesc), C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_eval_ld_batch.restype = C.c_int
         L.orc_max_threads.restype = C.c_int
         _libs[name] = L
     return _libs[name]
@@ -146,6 +149,22 @@ class Table:
         return _eval_ld(lambda v, g, lh, l2, x, y: getattr(lib(), f"orc_eval_ld_{self.kind}")(
             C.byref(self.desc), self.dims, form, ptr(cf), x, y, ptr(v), ptr(g), ptr(lh), ptr(l2)),
             self.dims, form, pos, self.dtype, self.N, self.ncomp)
+
+    def eval_ld_batch(self, pos, form: int = 2, coefs: np.ndarray = None, nthreads: int = 0, fast: bool = False):
+        """eval_ld for many points with OpenMP (the timed CPU path): same
+        outputs as eval_ld."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, self.dims)
+        P = pos.shape[0]
+        cf = self.coefs if coefs is None else np.ascontiguousarray(coefs)
+        ext = (2,) if self.ncomp == 2 else ()
+        v = np.zeros((P, self.N) + ext, self.dtype)
+        g = np.zeros((P, self.N) + ((2,) if self.dims == 2 else ()) + ext, self.dtype) if form >= 1 else None
+        h = None
+        if form >= 2:
+            h = np.zeros((P, self.N) + ((2, 2) if self.dims == 2 and form == 3 else ()) + ext, self.dtype)
+        lib(fast).orc_eval_ld_batch(ord(self.kind), self.dims, form, C.byref(self.desc), ptr(cf), P, ptr(pos),
+                                    ptr(v), ptr(g), ptr(h), nthreads)
+        return v, g, h
 
     def eval_vghgh(self, pos: np.ndarray, coefs: np.ndarray = None):
         """Value, gradient, Hessian and third derivatives [P][N][3][3][3]
