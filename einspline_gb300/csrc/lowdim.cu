@@ -3,7 +3,7 @@
 // alike) and the batched 1D GPU entries eval_multi_multi_UBspline_1d_*[_vgl]_cuda
 // (src/multi_bspline_cuda_s_impl.h:10-175, src/multi_bspline_cuda_c_impl.h:9-175).
 //
-// A block takes one point and kLdThreads * VW consecutive real columns; each
+// A block takes kLdPoints points and kLdThreads * VW consecutive real columns; each
 // thread reads its columns of the 4 (1D) or 16 (2D) stencil rows with one
 // vector load per row and reduces them separably (y first, then x), the
 // basis weights computed by every thread from the point's cell (a handful
@@ -16,6 +16,7 @@
 namespace eg {
 
 constexpr int kLdThreads = 128;
+constexpr int kLdPoints = 4;
 
 template <typename A>
 __device__ __forceinline__ void ld_axis(const EvalArgs &a, int64_t p, int ax, int dims, int &idx, A *w) {
@@ -29,18 +30,47 @@ __device__ __forceinline__ void ld_axis(const EvalArgs &a, int64_t p, int ax, in
   bspline_weights<A>(t, w, d);
 }
 
+// Stores VW values at p (16-byte vector stores when aligned and complete).
+template <typename A, int VW>
+__device__ __forceinline__ void st_row(A *p, int col0, int ncol, const A (&v)[VW]) {
+  if (col0 + VW <= ncol && al16(p)) {
+#pragma unroll
+    for (int c = 0; c < VW * (int)sizeof(A) / 16; c++) {
+      float4 q;
+      memcpy(&q, reinterpret_cast<const char *>(v) + 16 * c, 16);
+      reinterpret_cast<float4 *>(p)[c] = q;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < VW; e++)
+      if (col0 + e < ncol) p[e] = v[e];
+  }
+}
+
+template <int ST, int D, bool DER>
+__device__ __forceinline__ void eval_ld_point(const EvalArgs &a, int64_t p, int col0);
+
+template <int ST, int D, bool DER>
+__global__ void __launch_bounds__(kLdThreads) k_eval_ld(const EvalArgs a) {
+  constexpr int VW = CT<ST>::VW;
+  const int col0 = (blockIdx.y * kLdThreads + threadIdx.x) * VW;
+  if (col0 >= a.ncol) return;
+  // kLdPoints consecutive points per block: more loads in flight per warp
+  const int64_t p0 = (int64_t)blockIdx.x * kLdPoints;
+#pragma unroll 1
+  for (int q = 0; q < kLdPoints; q++)
+    if (p0 + q < a.npts) eval_ld_point<ST, D, DER>(a, p0 + q, col0);
+}
+
 // o (D = 1): value, first, second derivative.
 // o (D = 2): value, d/dx, d/dy, d2/dx2, d2/dxdy, d2/dy2.
 // a.out: 0 value, 1 vg, 2 vgl, 3 vgh; a.layout: 1 the CPU API's layouts at
 // flat bases with per-point strides, 0 the 1D GPU entries' pointer arrays
 // (value, gradient, second derivative per real column).
 template <int ST, int D, bool DER>
-__global__ void __launch_bounds__(kLdThreads) k_eval_ld(const EvalArgs a) {
+__device__ __forceinline__ void eval_ld_point(const EvalArgs &a, int64_t p, int col0) {
   using A = typename CT<ST>::A;
   constexpr int VW = CT<ST>::VW;
-  const int64_t p = blockIdx.x;
-  const int col0 = (blockIdx.y * kLdThreads + threadIdx.x) * VW;
-  if (col0 >= a.ncol) return;
   A wx[12], wy[12];
   int ix, iy = 0;
   ld_axis<A>(a, p, 0, D, ix, wx);
@@ -108,17 +138,17 @@ __global__ void __launch_bounds__(kLdThreads) k_eval_ld(const EvalArgs a) {
       for (int q = 0; q < 6; q++) o[q][e] *= sc;
     }
   }
+  if (a.layout == 0) {
+    st_row<A, VW>(reinterpret_cast<A *>(a.vals_pp[p]) + col0, col0, a.ncol, o[0]);
+    if (DER && a.out >= 1) st_row<A, VW>(reinterpret_cast<A *>(a.grads_pp[p]) + col0, col0, a.ncol, o[1]);
+    if (DER && a.out >= 2) st_row<A, VW>(reinterpret_cast<A *>(a.hess_pp[p]) + col0, col0, a.ncol, o[2]);
+    return;
+  }
   const int nc = a.is_complex ? 2 : 1;
 #pragma unroll
   for (int e = 0; e < VW; e++) {
     const int col = col0 + e;
     if (col >= a.ncol) break;
-    if (a.layout == 0) {
-      reinterpret_cast<A *>(a.vals_pp[p])[col] = o[0][e];
-      if (DER && a.out >= 1) reinterpret_cast<A *>(a.grads_pp[p])[col] = o[1][e];
-      if (DER && a.out >= 2) reinterpret_cast<A *>(a.hess_pp[p])[col] = o[2][e];
-      continue;
-    }
     // complex columns interleave re/im of one spline: entry m of spline n
     // sits at nc * (K * n + m) + part for a K-entry output
     const int n = col / nc, part = col - n * nc;
@@ -158,8 +188,9 @@ void launch_ld_st(const EvalArgs &a, int dims, dim3 grid, cudaStream_t s) {
 int launch_ld(Table *t, const EvalArgs &a, cudaStream_t s) {
   const int VW = t->storage == ST_F64 ? 2 : 4;
   const unsigned tiles = (unsigned)((t->ncol + kLdThreads * VW - 1) / (kLdThreads * VW));
-  if (a.npts > 0x7FFFFFFF) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call");
-  const dim3 grid((unsigned)a.npts, tiles);
+  const int64_t blocks = (a.npts + kLdPoints - 1) / kLdPoints;
+  if (blocks > 0x7FFFFFFF) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call");
+  const dim3 grid((unsigned)blocks, tiles);
   switch (t->storage) {
     case ST_F32: launch_ld_st<ST_F32>(a, t->dims, grid, s); break;
     case ST_F16: launch_ld_st<ST_F16>(a, t->dims, grid, s); break;
