@@ -9,7 +9,7 @@
 // (update_inverse_cuda1/2, src/determinant_update.h:9-111, launched at
 // src/cuda_walker.cu:92-136).
 //
-// k_det_ratio fuses the first two: one block per walker gathers the stencil
+// k_det_ratio fuses the first two: a block of 4 warps gathers the stencil
 // of all N orbitals with the evaluation kernels' separable reduction and
 // contracts value, gradient and Laplacian with the inverse column in
 // registers, so the per-orbital outputs never reach HBM (only the value row,
@@ -40,6 +40,11 @@ struct DetArgs {
 };
 
 constexpr int kDetThreads = 128;
+// Copy-pipeline depth: two stages keep a block at ~70 KB of shared memory so
+// three blocks (12 warps) share an SM; the register cap of the kernel
+// (launch bounds) matches.
+constexpr int kDetStages = 2;
+constexpr int kDetBlocksPerSM = 3;
 
 // Inverse entry (orbital j, electron c).
 __device__ __forceinline__ float ainv_at(const float *m, int j, int c, int ld, int trans) {
@@ -50,7 +55,7 @@ __device__ __forceinline__ float ainv_at(const float *m, int j, int c, int ld, i
 // sources for pb walkers, the copy pipeline, and per-warp partial sums.
 __host__ __device__ __forceinline__ size_t det_pipe_off(int pb) { return align_up(smem_total(pb, 4), 16); }
 __host__ __device__ __forceinline__ size_t det_red_off(int pb, int rb) {
-  return det_pipe_off(pb) + pipe_bytes(kDetThreads, rb);
+  return det_pipe_off(pb) + pipe_bytes(kDetThreads, rb, kDetStages);
 }
 __host__ __device__ __forceinline__ size_t det_ptr_off(int pb, int rb) {
   return align_up(det_red_off(pb, rb) + (size_t)pb * (kDetThreads / 32) * 5 * sizeof(float), 16);
@@ -74,7 +79,7 @@ __host__ __device__ __forceinline__ size_t det_smem(int pb, int rb) {
 // per walker adds the warps in order.  WIDE (16-bit tables): 8 columns and
 // one 16-byte copy per thread and row.
 template <int ST, bool GL, bool WIDE>
-__global__ void __launch_bounds__(kDetThreads) k_det_ratio(const DetArgs d) {
+__global__ void __launch_bounds__(kDetThreads, kDetBlocksPerSM) k_det_ratio(const DetArgs d) {
   using Raw = typename CT<ST>::Raw;
   static_assert(sizeof(typename CT<ST>::A) == 4, "determinant step: real float tables only");
   constexpr int VW = WIDE ? 2 * CT<ST>::VW : CT<ST>::VW;
@@ -109,7 +114,7 @@ __global__ void __launch_bounds__(kDetThreads) k_det_ratio(const DetArgs d) {
     if ((g * kDetThreads + (int)threadIdx.x) * VW >= d.n) return;
     const char *plane = cbase + (int64_t)g * GC * CT<ST>::BYTES + (sidx[3 * pp] + i) * xsb +
                         sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
-    const unsigned dst = my + (unsigned)(st % kPipeStages) * slot_step;
+    const unsigned dst = my + (unsigned)(st % kDetStages) * slot_step;
 #pragma unroll
     for (int r = 0; r < 16; r++) cp_async<RB>(dst + r * row_step, plane + (r >> 2) * ysb + (r & 3) * zsb);
     if (i == 0) {
@@ -128,7 +133,7 @@ __global__ void __launch_bounds__(kDetThreads) k_det_ratio(const DetArgs d) {
     }
   };
 #pragma unroll
-  for (int st = 0; st < kPipeStages - 1; st++) {
+  for (int st = 0; st < kDetStages - 1; st++) {
     if (st < S) issue(st);
     cp_async_commit();
   }
@@ -138,9 +143,9 @@ __global__ void __launch_bounds__(kDetThreads) k_det_ratio(const DetArgs d) {
   float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   float av[VW];
   for (int st = 0; st < S; st++) {
-    if (st + kPipeStages - 1 < S) issue(st + kPipeStages - 1);
+    if (st + kDetStages - 1 < S) issue(st + kDetStages - 1);
     cp_async_commit();
-    cp_async_wait<kPipeStages - 1>();
+    cp_async_wait<kDetStages - 1>();
     const int i = st & 3, rest = st >> 2, g = rest % G, pp = rest / G;
     const int col0 = (g * kDetThreads + (int)threadIdx.x) * VW;
     const bool live = col0 < d.n;
@@ -153,7 +158,7 @@ __global__ void __launch_bounds__(kDetThreads) k_det_ratio(const DetArgs d) {
       }
     }
     if (live) {
-      const unsigned char *slot = pipe + (size_t)(st % kPipeStages) * slot_step + (size_t)threadIdx.x * RB;
+      const unsigned char *slot = pipe + (size_t)(st % kDetStages) * slot_step + (size_t)threadIdx.x * RB;
       reduce_plane<float, VW, GL>(
           i, w, wz,
           [&](int j, int k, float(&c)[VW]) {
@@ -414,12 +419,12 @@ int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_de
   d.trans = o->ainv_trans;
   const bool gl = grad_d || lapl_d;
   cudaStream_t s = stream ? (cudaStream_t)stream : cudaStreamLegacy;
-  // Two blocks fit on an SM (their copy pipelines take 96 KB each).  The
-  // walkers are spread evenly over at most one wave of such blocks, so each
-  // block runs one long pipeline over its walkers (no per-block fill and
-  // drain for every walker, no partial last wave); beyond 32 walkers per
-  // block the grid grows instead.
-  const int slots = 2 * num_sms();
+  // kDetBlocksPerSM blocks fit on an SM.  The walkers are spread evenly
+  // over at most one wave of such blocks, so each block runs one long
+  // pipeline over its walkers (no per-block fill and drain for every walker,
+  // no partial last wave); beyond 32 walkers per block the grid grows
+  // instead.
+  const int slots = kDetBlocksPerSM * num_sms();
   int pb = (nwalkers + slots - 1) / slots;
   pb = pb < 1 ? 1 : (pb > 32 ? 32 : pb);
   d.e.pb = pb;
