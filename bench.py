@@ -569,8 +569,8 @@ def lowdim_1d(P=262144, reps=10):
 
 def other_configs(args):
     """Throughput of the other workloads (parity-test configurations, not
-    the headline): C2 FP64 48^3 x 512 plane waves, 128 x 256 points; C3
-    complex 64^3 x 256, 256 x 128 points, random vs cell-sorted; C5 FP32/F16
+    the headline): FP64 48^3 x 512 plane waves, 128 x 256 points; complex
+    64^3 x 256, 256 x 128 points, random vs cell-sorted; FP32/F16
     128^3 x 2048, chunks of 256 walkers x 256 points."""
     import torch
     from einspline_gb300 import api, synth
@@ -608,7 +608,7 @@ def other_configs(args):
     t.set_fp64_mode(1)
     r_df = rate(t, p)
     t.set_fp64_mode(0)
-    out["C2_d_48cube_512"] = {"evals_per_s": r, "GBps_alg": r * 592 / 1e9, "tile": list(t.get_tile()),
+    out["d_48cube_512"] = {"evals_per_s": r, "GBps_alg": r * 592 / 1e9, "tile": list(t.get_tile()),
                               "double_float": {"evals_per_s": r_df, "GBps_alg": r_df * 592 / 1e9,
                                                "note": "einspline_gb300_set_fp64_mode(1): FP64 table, "
                                                        "double-float arithmetic (tested to 1e-12 of FP64)"}}
@@ -616,7 +616,7 @@ def other_configs(args):
     t = dev_table("c", 64, 256, 303)
     t.autotune(256 * 128)
     p = torch.from_numpy(synth.points_uniform(304, 256 * 128)).cuda()
-    out["C3_c_64cube_256"] = {"random_evals_per_s": rate(t, p), "sorted_evals_per_s": rate(t, p, sort=True),
+    out["c_64cube_256"] = {"random_evals_per_s": rate(t, p), "sorted_evals_per_s": rate(t, p, sort=True),
                               "GBps_alg_random": rate(t, p) * 592 / 1e9}
     del t
     out["ld1_s_512_1024"] = lowdim_1d()
@@ -628,7 +628,7 @@ def other_configs(args):
         bufs = (torch.empty((P, 2048), device="cuda"), torch.empty((P, 2048, 3), device="cuda"),
                 torch.empty((P, 2048, 6), device="cuda"))
         r = rate(t, p, reps=3, out_bufs=bufs)
-        out[f"C5_s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9,
+        out[f"s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9,
                                             "note": "256 walkers x 256 points per launch (the 4096-walker step "
                                                     "is 16 such launches; outputs of all 4096 would be 84 GB)"}
         del t, bufs

@@ -2,7 +2,7 @@
 
 Each translation unit in csrc/ is compiled by nvcc for sm_103a in parallel and
 linked into one shared library with the CUDA runtime linked statically, so the
-only run-time dependency is the driver.  Host code is compiled without FMA
+only run-time dependency is the CUDA driver.  Host code is compiled without FMA
 contraction (the host copy of the line solve must match the oracle bit for bit).
 """
 from __future__ import annotations

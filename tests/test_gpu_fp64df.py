@@ -86,7 +86,7 @@ def test_df_mode_errors(orc):
 
 
 @pytest.mark.gpu
-def test_df_c2_double_planewaves_full_size(orc):
+def test_df_planewaves_48cube_512(orc):
     """The 48^3 x 512 FP64 plane-wave workload (128 walkers x 256 points):
     double-float results against the IEEE FP64 path at full size, and
     against the oracle on sampled columns."""
@@ -109,4 +109,4 @@ def test_df_c2_double_planewaves_full_size(orc):
         T.set_spline(j, data[c])
     sub = np.arange(0, 128 * 256, 64)
     ref = cpu_to_gpu_layout("d", *T.eval(pos.cpu().numpy()[sub], sem=0))
-    assert_close((got[0][sub][:, cols], got[1][sub][:, cols], got[2][sub][:, cols]), ref, TOL["d"], "C2 df")
+    assert_close((got[0][sub][:, cols], got[1][sub][:, cols], got[2][sub][:, cols]), ref, TOL["d"], "48^3 df")

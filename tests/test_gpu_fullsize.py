@@ -72,7 +72,7 @@ def check_nodes(G, kind, M, N, seed, npts, tol):
 
 
 @pytest.mark.gpu
-def test_c2_double_planewaves_full_size(orc):
+def test_fp64_planewaves_48cube_512(orc):
     """multi_UBspline_3d_d, periodic 48^3, 512 splines of 8 plane waves plus
     noise; 128 walkers x 256 points vgh in one batched launch."""
     import torch
@@ -90,7 +90,7 @@ def test_c2_double_planewaves_full_size(orc):
         T.set_spline(j, data[c])
     sub = np.arange(0, pos.shape[0], 64)
     ref = cpu_to_gpu_layout("d", *T.eval(pos[sub], sem=0))
-    assert_close((v[sub][:, cols], g[sub][:, cols], h[sub][:, cols]), ref, TOL["d"], "C2 sampled")
+    assert_close((v[sub][:, cols], g[sub][:, cols], h[sub][:, cols]), ref, TOL["d"], "FP64 48^3 sampled")
     # interpolation at nodes, all 512 splines
     rng = np.random.default_rng(5)
     nodes = rng.integers(0, 48, size=(64, 3))
@@ -100,7 +100,7 @@ def test_c2_double_planewaves_full_size(orc):
 
 
 @pytest.mark.gpu
-def test_c3_complex_sorted_full_size(orc):
+def test_complex_64cube_256_sorted(orc):
     """multi_UBspline_3d_c, periodic 64^3, 256 complex splines (0.6 GB);
     256 walkers x 128 points vgh; sorted by cell vs random order."""
     import torch
@@ -117,7 +117,7 @@ def test_c3_complex_sorted_full_size(orc):
     sub = np.arange(0, pos.shape[0], 128)
     ref = cpu_to_gpu_layout("z", *T.eval(pos[sub], sem=0))
     got = (a[0][sub][:, cols], a[1][sub][:, cols], a[2][sub][:, cols])
-    assert_close(got, ref, F32_VS_F64, "C3 sampled vs FP64")
+    assert_close(got, ref, F32_VS_F64, "complex 64^3 sampled vs FP64")
     check_nodes(G, "c", M, N, seed, 128, F32_VS_F64)
 
 
@@ -139,7 +139,7 @@ def rel_l2(a, b):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16, api.STORE_I16, api.STORE_BF16])
-def test_c4_serving_table_errors_vs_fp64(orc, storage):
+def test_serving_table_64cube_1024_errors_vs_fp64(orc, storage):
     """multi_UBspline_3d_s, 64^3, 1024 splines: FP32 and 16-bit tables
     against the FP64 solve and evaluation on sampled columns."""
     import torch
@@ -158,7 +158,7 @@ def test_c4_serving_table_errors_vs_fp64(orc, storage):
 
 
 @pytest.mark.gpu
-def test_c5_large_table_int64_offsets(orc):
+def test_large_table_128cube_2048_int64_offsets(orc):
     """multi_UBspline_3d_s, 128^3, 2048 splines: 4.6e9 table elements
     (18.4 GB FP32), beyond 32-bit offsets; sampled columns vs FP64."""
     import torch
@@ -172,19 +172,19 @@ def test_c5_large_table_int64_offsets(orc):
     T = sampled_oracle(orc, "s", grids, M, seed, cols)
     sub = np.arange(0, 4096, 16)
     ref = cpu_to_gpu_layout("d", *T.eval(pos[sub], sem=0))
-    assert_close((v[sub][:, cols], g[sub][:, cols], h[sub][:, cols]), ref, 4 * F32_VS_F64, "C5 sampled vs FP64")
+    assert_close((v[sub][:, cols], g[sub][:, cols], h[sub][:, cols]), ref, 4 * F32_VS_F64, "128^3 sampled vs FP64")
     # the high corner of the table (offsets past 2^32 elements)
     corner = np.array([[0.999, 0.999, 0.999], [0.995, 0.5, 0.999]])
     vc = G.eval(torch.from_numpy(corner).cuda(), rule=0, layout=0)
     ref_c = cpu_to_gpu_layout("d", *T.eval(corner, sem=0))
     assert_close((vc[0].cpu().numpy()[:, cols], vc[1].cpu().numpy()[:, cols], vc[2].cpu().numpy()[:, cols]),
-                 ref_c, 4 * F32_VS_F64, "C5 corner")
+                 ref_c, 4 * F32_VS_F64, "128^3 corner")
     del G
     torch.cuda.empty_cache()
 
 
 @pytest.mark.gpu
-def test_c1_cpu_plain_config(orc):
+def test_plain_32cube_128_value_and_vgh(orc):
     """multi_UBspline_3d_s, periodic 32^3, 128 splines, 10,000 points, value
     and vgh, against the FP64 evaluation of the same data."""
     import torch
@@ -203,4 +203,4 @@ def test_c1_cpu_plain_config(orc):
     v, g, h = (x.cpu().numpy() for x in G.eval(pt, rule=0, layout=1))
     rv, rg, rh = T.eval(pos, sem=0)
     assert np.array_equal(val, v)
-    assert_close((v, g, h), (rv, rg, rh), F32_VS_F64, "C1 vs FP64")
+    assert_close((v, g, h), (rv, rg, rh), F32_VS_F64, "32^3 vs FP64")
