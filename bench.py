@@ -523,6 +523,19 @@ def det_step(tabs, W=2048, reps=20):
     out["update"] = {"accepted": len(acc), "ms": ms_u, "GBps_alg": len(acc) * 3 * N * N * 4 / (ms_u / 1e3) / 1e9}
     del A, Ai, D
     torch.cuda.empty_cache()
+    # A large population, ratio kernel only: with k = 0 a transposed inverse
+    # is read only in its row 0, so a [W][1][N] buffer stands for W matrices.
+    Wl = 16384
+    Ai1 = torch.empty((Wl, 1, N), dtype=torch.float32, device="cuda")
+    api.fill_uniform(Ai1, 94, -1.0, 1.0)
+    Dl = api.Determinants(Ai1, Ai1, N, trans=1)
+    posl = [torch.from_numpy(synth.points_uniform(95 + i, Wl).astype(np.float32)).cuda() for i in range(reps + 3)]
+    pos = posl
+    ms_l = timeit(lambda p: Dl.ratio(tabs["f16"], p, 0, grad_lapl=True))
+    out["f16_ratio_16384_walkers"] = {"ms": ms_l, "orbital_evals_per_s": Wl * N / (ms_l / 1e3),
+                                      "GBps_alg": Wl * N * 132 / (ms_l / 1e3) / 1e9}
+    del Ai1, Dl, posl, pos
+    torch.cuda.empty_cache()
     return out
 
 

@@ -9,13 +9,18 @@
 //    device-memory arena (first-fit free list), packs admitted requests into
 //    a batch of at most max_batch_points and launches it on one of
 //    max_inflight slots, each with its own stream, pinned staging buffer and
-//    instantiated CUDA graph (copy-in -> evaluation kernel -> host callback);
-//  * the host callback stamps completion times and frees the slot, so new
-//    requests join the next batch while earlier batches are still running;
+//    instantiated CUDA graph (copy-in -> evaluation kernel -> event record);
+//  * a completion thread polls the in-flight batches' events, stamps
+//    completion times and frees the slot, so new requests join the next
+//    batch while earlier batches are still running; it sleeps when nothing
+//    is in flight, and the worker spins ~100 us before it sleeps: the two
+//    thread wake-ups a request would otherwise wait for cost tens of
+//    microseconds each, more than the evaluation of a walker;
 //  * release() returns a request's outputs to the arena and wakes admission.
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -86,8 +91,10 @@ struct Slot {
   char *stage_h = nullptr, *stage_d = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  cudaGraphNode_t n_copy = nullptr, n_kernel = nullptr, n_host = nullptr;
+  cudaGraphNode_t n_copy = nullptr, n_kernel = nullptr, n_event = nullptr;
+  cudaEvent_t done = nullptr;  // recorded after the batch's kernel
   bool busy = false;
+  bool launched = false;       // the batch (and its event record) is enqueued
   std::vector<int64_t> reqs;
   int64_t points = 0;
 };
@@ -110,7 +117,15 @@ struct Server {
   char *arena_d = nullptr;
   Arena arena;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work, cv_done, cv_poll;
+  // bumped, under mu, whenever the worker may have something new to do (a
+  // submit, a finished batch, released memory): the worker spins on it
+  // briefly before it blocks
+  std::atomic<uint64_t> epoch{0};
+  int device = 0;
+  int launched = 0;            // slots launched and not yet seen complete
+  bool stop_poll = false;
+  std::thread poller;
   std::deque<int64_t> queue, admitted;
   std::unordered_map<int64_t, Request> reqs;
   std::vector<Slot> slots;
@@ -127,24 +142,57 @@ struct Server {
   size_t stage_bytes() const { return (size_t)o.max_batch_points * (24 + pos_b); }
 };
 
-static void CUDART_CB on_batch_done(void *p) {
-  Slot *s = (Slot *)p;
-  Server *v = s->srv;
-  const double t = now_s();
-  {
-    std::lock_guard<std::mutex> g(v->mu);
-    for (int64_t id : s->reqs) {
-      auto it = v->reqs.find(id);
-      if (it != v->reqs.end()) { it->second.state = 3; it->second.t_done = t; }
-    }
-    v->st.completed += (int64_t)s->reqs.size();
-    s->reqs.clear();
-    s->busy = false;
-    v->inflight--;
-    v->t_last = t;
+// Marks a batch's requests done (under the server lock).
+static void complete_locked(Server *v, Slot &s, double t) {
+  for (int64_t id : s.reqs) {
+    auto it = v->reqs.find(id);
+    if (it != v->reqs.end()) { it->second.state = 3; it->second.t_done = t; }
   }
-  v->cv_done.notify_all();
-  v->cv_work.notify_one();
+  v->st.completed += (int64_t)s.reqs.size();
+  s.reqs.clear();
+  s.busy = false;
+  s.launched = false;
+  v->launched--;
+  v->inflight--;
+  v->t_last = t;
+}
+
+// Completion thread: while batches are in flight it polls their events
+// (a few microseconds from the GPU finishing to the requests being marked
+// done, against a host-callback thread's wake-up); with nothing in flight it
+// sleeps.  It leaves only when stopped and every launched batch is done.
+static void poller_loop(Server *v) {
+  cudaSetDevice(v->device);
+  std::vector<Slot *> live;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(v->mu);
+      v->cv_poll.wait(lk, [&] { return v->launched > 0 || v->stop_poll; });
+      if (v->launched == 0) return;  // stopped and drained
+      live.clear();
+      for (auto &sl : v->slots)
+        if (sl.busy && sl.launched) live.push_back(&sl);
+    }
+    bool any = false;
+    for (Slot *sl : live) {
+      const cudaError_t e = cudaEventQuery(sl->done);
+      if (e == cudaErrorNotReady) continue;
+      const double t = now_s();
+      {
+        std::lock_guard<std::mutex> g(v->mu);
+        if (e != cudaSuccess && v->worker_error.empty()) v->worker_error = cudaGetErrorString(e);
+        complete_locked(v, *sl, t);
+        v->epoch.fetch_add(1);
+      }
+      any = true;
+    }
+    if (any) {
+      v->cv_done.notify_all();
+      v->cv_work.notify_one();
+    } else {
+      std::this_thread::yield();
+    }
+  }
 }
 
 // Packed staging of a batch of n points: vals_pp[n], grads_pp[n], hess_pp[n],
@@ -181,10 +229,7 @@ static int build_graph(Server *v, Slot &s) {
   kp.sharedMemBytes = (unsigned)smem;
   kp.kernelParams = args;
   EG_CUDA(cudaGraphAddKernelNode(&s.n_kernel, s.graph, &s.n_copy, 1, &kp));
-  cudaHostNodeParams hp;
-  hp.fn = on_batch_done;
-  hp.userData = &s;
-  EG_CUDA(cudaGraphAddHostNode(&s.n_host, s.graph, &s.n_kernel, 1, &hp));
+  EG_CUDA(cudaGraphAddEventRecordNode(&s.n_event, s.graph, &s.n_kernel, 1, s.done));
   EG_CUDA(cudaGraphInstantiate(&s.exec, s.graph, 0));
   v->func = func;
   return 0;
@@ -215,12 +260,16 @@ static int launch_batch(Server *v, Slot &s) {
   } else {
     EG_CUDA(cudaMemcpyAsync(s.stage_d, s.stage_h, bytes, cudaMemcpyHostToDevice, s.stream));
     if (int r = launch_eval(v->t, a, v->o.vgh != 0, s.stream, v->tx, v->ty, v->pb)) return r;
-    EG_CUDA(cudaLaunchHostFunc(s.stream, on_batch_done, &s));
+    EG_CUDA(cudaEventRecord(s.done, s.stream));
   }
   return 0;
 }
 
+// Spin budget of the worker before it blocks on its condition variable.
+constexpr double kSpinSeconds = 100e-6;
+
 static void worker_loop(Server *v) {
+  cudaSetDevice(v->device);
   const size_t ncol = v->t->ncol;
   for (;;) {
     Slot *slot = nullptr;
@@ -243,7 +292,15 @@ static void worker_loop(Server *v) {
           for (auto &s : v->slots)
             if (!s.busy) { slot = &s; break; }
         if (slot) break;
-        v->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+        // nothing to launch: spin briefly on the epoch (a thread wake-up
+        // costs tens of microseconds), then block
+        const uint64_t seen = v->epoch.load();
+        lk.unlock();
+        const double t_spin = now_s() + kSpinSeconds;
+        while (v->epoch.load() == seen && now_s() < t_spin) std::this_thread::yield();
+        lk.lock();
+        if (v->epoch.load() == seen && !v->stop)
+          v->cv_work.wait_for(lk, std::chrono::milliseconds(50), [&] { return v->epoch.load() != seen || v->stop; });
       }
       // form a batch from admitted requests
       slot->reqs.clear();
@@ -286,6 +343,13 @@ static void worker_loop(Server *v) {
       slot->busy = false;
       v->inflight--;
       v->cv_done.notify_all();
+    } else {
+      {
+        std::lock_guard<std::mutex> g(v->mu);
+        slot->launched = true;
+        v->launched++;
+      }
+      v->cv_poll.notify_one();
     }
   }
 }
@@ -335,6 +399,7 @@ einspline_gb300_server *einspline_gb300_server_create(einspline_gb300_table *t, 
     else cuda_check(cudaGetLastError(), what);
     return nullptr;
   };
+  cudaGetDevice(&v->device);
   if (cudaMalloc(&v->arena_d, budget) != cudaSuccess) return bail("server arena");
   v->arena.reset(budget);
   v->st.budget_bytes = budget;
@@ -344,10 +409,12 @@ einspline_gb300_server *einspline_gb300_server_create(einspline_gb300_table *t, 
     s.srv = v;
     if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMallocHost(&s.stage_h, v->stage_bytes()) != cudaSuccess ||
-        cudaMalloc(&s.stage_d, v->stage_bytes()) != cudaSuccess)
+        cudaMalloc(&s.stage_d, v->stage_bytes()) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess)
       return bail("server slot");
     if (v->o.use_graphs && build_graph(v, s)) return bail("server graph");
   }
+  v->poller = std::thread(poller_loop, v);
   v->worker = std::thread(worker_loop, v);
   auto *h = new einspline_gb300_server();
   h->impl = v;
@@ -379,8 +446,16 @@ void destroy_server(Server *v) {
   }
   v->cv_work.notify_all();
   if (v->worker.joinable()) v->worker.join();
+  {
+    // the poller drains the launched batches, then leaves
+    std::lock_guard<std::mutex> g(v->mu);
+    v->stop_poll = true;
+  }
+  v->cv_poll.notify_all();
+  if (v->poller.joinable()) v->poller.join();
   for (auto &sl : v->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
+    if (sl.done) cudaEventDestroy(sl.done);
     if (sl.exec) cudaGraphExecDestroy(sl.exec);
     if (sl.graph) cudaGraphDestroy(sl.graph);
     if (sl.stage_h) cudaFreeHost(sl.stage_h);
@@ -422,6 +497,7 @@ int64_t einspline_gb300_server_submit(einspline_gb300_server *s, const void *pos
     v->reqs.emplace(id, std::move(r));
     v->queue.push_back(id);
     v->st.submitted++;
+    v->epoch.fetch_add(1);  // under the lock: the worker's wait cannot miss it
   }
   v->cv_work.notify_one();
   return id;
@@ -490,6 +566,7 @@ int einspline_gb300_server_release(einspline_gb300_server *s, int64_t id) {
     v->arena.release(it->second.off, it->second.bytes);
     v->reqs.erase(it);
     v->st.released++;
+    v->epoch.fetch_add(1);
   }
   v->cv_work.notify_one();
   return 0;
