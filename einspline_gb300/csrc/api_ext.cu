@@ -164,6 +164,11 @@ int einspline_gb300_set_fp64_mode(einspline_gb300_table *t, int mode) {
   if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle (3D tables only)");
   if (mode != 0 && mode != 1) return fail(EINSPLINE_GB300_EINVAL, "mode must be 0 or 1");
   if (t->storage != ST_F64) return mode ? fail(EINSPLINE_GB300_EINVAL, "not an FP64 (d/z) table") : 0;
+  {
+    std::lock_guard<std::mutex> lock(t->mu);
+    if (t->servers > 0 && mode != t->fp64_mode)
+      return fail(EINSPLINE_GB300_EBUSY, "a request server uses this table: set the mode before creating it");
+  }
   if (int r = table_flush(t)) return r;
   {
     std::lock_guard<std::mutex> lock(t->mu);

@@ -92,6 +92,7 @@ struct einspline_gb300_table {
   int fp64_mode = 0;
   void *df_coefs = nullptr;         // device, table_bytes
   bool df_stale = true;
+  int servers = 0;                  // request servers built on this table
   bool owns = true;
 
   // queued set calls

@@ -414,6 +414,10 @@ einspline_gb300_server *einspline_gb300_server_create(einspline_gb300_table *t, 
       return bail("server slot");
     if (v->o.use_graphs && build_graph(v, s)) return bail("server graph");
   }
+  {
+    std::lock_guard<std::mutex> g(t->mu);
+    t->servers++;
+  }
   v->poller = std::thread(poller_loop, v);
   v->worker = std::thread(worker_loop, v);
   auto *h = new einspline_gb300_server();
@@ -425,6 +429,10 @@ int einspline_gb300_server_destroy(einspline_gb300_server *s) {
   clear();
   Server *v = srv_of(s);
   if (!v) return EINSPLINE_GB300_EINVAL;
+  {
+    std::lock_guard<std::mutex> g(v->t->mu);
+    v->t->servers--;
+  }
   destroy_server(v);
   s->magic = 0;
   s->impl = nullptr;

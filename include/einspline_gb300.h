@@ -300,7 +300,9 @@ int einspline_gb300_det_update(const einspline_gb300_det_opts *opts, int naccept
  *     table's size again), rebuilt after set_* / flush.
  * Applies to every 3D evaluation of the table (flat, host-buffer, server,
  * single-point and *_cuda entries of a handle made from it take the handle's
- * own table: set the mode on c->gb300).  Not for 1D/2D tables. */
+ * own table: set the mode on c->gb300).  Not for 1D/2D tables.  A request
+ * server captures the table's kernel in its graphs: set the mode before
+ * creating one (changing it while a server exists fails with EBUSY). */
 int einspline_gb300_set_fp64_mode(einspline_gb300_table *t, int mode);
 int einspline_gb300_get_fp64_mode(einspline_gb300_table *t);
 

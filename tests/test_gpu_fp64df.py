@@ -110,3 +110,26 @@ def test_df_planewaves_48cube_512(orc):
     sub = np.arange(0, 128 * 256, 64)
     ref = cpu_to_gpu_layout("d", *T.eval(pos.cpu().numpy()[sub], sem=0))
     assert_close((got[0][sub][:, cols], got[1][sub][:, cols], got[2][sub][:, cols]), ref, TOL["d"], "48^3 df")
+
+
+@pytest.mark.gpu
+def test_df_server(orc):
+    """A request server on a double-float table returns FP64-tolerance
+    results; the mode cannot change under a running server."""
+    grids, bcs = CASES["mixed"]
+    G, T, _ = build_pair(orc, "d", grids, bcs, 9, seed=531)
+    G.set_fp64_mode(1)
+    S = api.Server(G, vgh=True, pos_f64=True, rule=0)
+    lo, hi = table_box(grids)
+    reqs = [synth.points_uniform(532 + i, 40 + 17 * i, lo, hi) for i in range(5)]
+    ids = [S.submit(p) for p in reqs]
+    for rid, p in zip(ids, reqs):
+        S.wait(rid)
+        v, g, h = S.result(rid, p.shape[0])
+        rv, rg, rh = cpu_to_gpu_layout("d", *T.eval(p, vgh=True, sem=0))
+        assert_close((v, g.reshape(rg.shape), h.reshape(rh.shape)), (rv, rg, rh), TOL["d"], "server df")
+        S.release(rid)
+    with pytest.raises(api.EinsplineError):
+        G.set_fp64_mode(0)
+    S.close()
+    G.set_fp64_mode(0)
