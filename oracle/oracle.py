@@ -504,6 +504,26 @@ def det_ratio_bound(vals, grads, hess, ainv, k):
     return sr, sg, sl
 
 
+REF_DET_LIB = os.path.join(HERE, "_ref", "libdetupdate_ref.so")
+
+
+def ref_det_update(ainv, delta, k):
+    """The reference's host update_inverse (src/determinant_update.cu:171-187,
+    float): its array, read as M[i][j] = X[j*N + i], is the inverse of a
+    matrix whose column k changes by delta; with X = Ainv[j][e] (orbital j,
+    electron e) row-major that is our row-k change of A.  N <= 128 (its
+    scratch arrays).  Returns the updated Ainv (float32)."""
+    L = C.CDLL(REF_DET_LIB)
+    f = getattr(L, "_Z14update_inversePfS_ii")  # C++ linkage: update_inverse(float*, float*, int, int)
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+    X = np.ascontiguousarray(ainv, dtype=np.float32).copy()
+    d = np.ascontiguousarray(delta, dtype=np.float32)
+    N = X.shape[0]
+    assert X.shape == (N, N) and N <= 128
+    f(ptr(X), ptr(d), N, int(k))
+    return X
+
+
 def sm_update(A, ainv, k, u):
     """Sherman-Morrison row update of one walker in float64: returns (A', Ainv')."""
     A = np.array(A, np.float64)

@@ -6,7 +6,9 @@ Each 3D case stores the seeded input data, the table the reference's
 set_multi_UBspline_3d_* produced (its float solve for s/c, double for d/z),
 evaluation points, and the reference's eval_multi_UBspline_3d_*, _vgh and
 _vghgh outputs at those points.  The ld1_*/ld2_* cases do the same for the
-1D and 2D multi-splines (value, vg, vgl and vgh forms).  The tests then pin the
+1D and 2D multi-splines (value, vg, vgl and vgh forms); det_update holds the
+reference's host Sherman-Morrison update (src/determinant_update.cu:171-187)
+on seeded inputs.  The tests then pin the
 oracle against these vectors on machines where the reference cannot be built.
 
 Run from the repository root:  python tests/golden/make_golden.py
@@ -95,9 +97,22 @@ def make_ld_case(kind, grids, bcs, N, npts, seed):
                 num_splines=np.array(N), data=data, table=R.table(), pos=pos, **out)
 
 
+def make_det_case(seed=3000):
+    """The reference's own Sherman-Morrison host update on seeded inputs."""
+    rng = np.random.default_rng(seed)
+    N, k = 48, 11
+    A = (rng.standard_normal((N, N)) + 6 * np.eye(N)).astype(np.float32)
+    ainv = np.linalg.inv(A.astype(np.float64)).astype(np.float32)
+    u = rng.standard_normal(N).astype(np.float32)
+    delta = (u - A[k]).astype(np.float32)
+    return dict(A=A, ainv=ainv, u=u, k=np.array(k), ainv_ref=O.ref_det_update(ainv, delta, k))
+
+
 def main():
     if not O.ref_available():
         sys.exit("reference library missing: run `make -C oracle ref` first")
+    np.savez_compressed(os.path.join(HERE, "det_update.npz"), **make_det_case())
+    print("wrote det_update")
     for k, (name, kind, grids, bcs, N, npts) in enumerate(CASES):
         case = make_case(name, kind, grids, bcs, N, npts, seed=1000 + 17 * k)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **case)

@@ -189,3 +189,23 @@ def test_det_errors(orc):
     Gd, _, _ = build_pair(orc, "d", GRIDS, [(P, P)] * 3, 8, seed=333)
     with pytest.raises(api.EinsplineError):
         D.ratio(Gd, pos, 0)             # FP64 tables are not taken
+
+
+@pytest.mark.gpu
+def test_det_update_matches_reference_fixture(orc):
+    """The GPU update against the reference's own host update_inverse
+    (src/determinant_update.cu:171-187) on the committed fixture."""
+    import os
+    torch = pytest.importorskip("torch")
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "det_update.npz"))
+    A, ainv, u, k = z["A"], z["ainv"], z["u"], int(z["k"])
+    N = A.shape[0]
+    D = api.Determinants(torch.from_numpy(A[None].copy()).cuda(), torch.from_numpy(ainv[None].copy()).cuda(), N,
+                         trans=0)
+    rows = torch.from_numpy(u[None].copy()).cuda()
+    D.update(k, [0], rows)
+    torch.cuda.synchronize()
+    got = D.ainv.cpu().numpy()[0].astype(np.float64)
+    ref = z["ainv_ref"].astype(np.float64)
+    assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
+    assert np.array_equal(D.A.cpu().numpy()[0][k], u)

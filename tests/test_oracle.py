@@ -9,7 +9,9 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
-                if not os.path.basename(p).startswith("ld"))
+                if not os.path.basename(p).startswith(("ld", "det")))
+GOLDEN_DET = os.path.join(HERE, "golden", "det_update.npz")
+REF_DET_BUILT = os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libdetupdate_ref.so"))
 GOLDEN_LD = sorted(glob.glob(os.path.join(HERE, "golden", "ld*.npz")))
 REF_BUILT = os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libeinspline_ref.so"))
 
@@ -183,3 +185,25 @@ def test_live_reference_lowdim(orc, kind):
             for a, b in zip(T.eval_ld(pos, form), R.eval_ld(pos, form)):
                 if a is not None:
                     assert np.array_equal(a, b)
+
+
+def test_golden_det_update(orc):
+    """The Sherman-Morrison restatement against the reference's own host
+    update_inverse (float) on the committed fixture."""
+    z = np.load(GOLDEN_DET)
+    k = int(z["k"])
+    _, got = orc.sm_update(z["A"], z["ainv"], k, z["u"])
+    ref = z["ainv_ref"].astype(np.float64)
+    assert np.abs(got - ref).max() <= 5e-6 * np.abs(ref).max()
+
+
+@pytest.mark.skipif(not REF_DET_BUILT, reason="reference determinant update not built here (make -C oracle ref)")
+@pytest.mark.parametrize("N,k", [(8, 0), (37, 20), (128, 127)])
+def test_live_reference_det_update(orc, N, k):
+    rng = np.random.default_rng(N + k)
+    A = (rng.standard_normal((N, N)) + 6 * np.eye(N)).astype(np.float32)
+    ainv = np.linalg.inv(A.astype(np.float64)).astype(np.float32)
+    u = rng.standard_normal(N).astype(np.float32)
+    ref = orc.ref_det_update(ainv, u - A[k], k).astype(np.float64)
+    _, got = orc.sm_update(A, ainv, k, u)
+    assert np.abs(got - ref).max() <= 5e-6 * np.abs(ref).max()
