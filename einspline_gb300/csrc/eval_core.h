@@ -202,6 +202,31 @@ __device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &
   }
 }
 
+// ------------------------------------------------------------ packed FP32
+// Blackwell's 2-wide FP32 instructions (PTX fma.rn.f32x2 / mul.rn.f32x2):
+// each lane is the IEEE round-to-nearest operation of the scalar code, so a
+// pair of columns sharing one weight costs one instruction instead of two
+// and gives bit-identical results.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk2(f32x2 r, float &a, float &b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
 // Separable reduction of the 4x4x4 stencil for VW columns.
 // w: [0..11] x weights, [12..23] y weights, [24..35] z weights.
 // o: v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz.
@@ -209,6 +234,67 @@ __device__ __forceinline__ void cell(const EvalArgs &a, int ax, double xd, int &
 // then this plane's x terms are added to o.
 template <typename A, int VW, bool VGH, typename RowFn>
 __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3][4], RowFn row, A (&o)[10][VW]) {
+  if constexpr (std::is_same<A, float>::value && VW % 2 == 0) {
+    // the same operations on column pairs, two lanes per instruction
+    constexpr int H = VW / 2;
+    f32x2 wz2[3][4];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+      for (int k = 0; k < 4; k++) wz2[d][k] = pk2(wz[d][k], wz[d][k]);
+    f32x2 y[6][H];
+#pragma unroll
+    for (int q = 0; q < 6; q++)
+#pragma unroll
+      for (int e = 0; e < H; e++) y[q][e] = pk2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      A c[4][VW];
+#pragma unroll
+      for (int k = 0; k < 4; k++) row(j, k, c[k]);
+      const f32x2 by = pk2(w[12 + j], w[12 + j]), dby = pk2(w[16 + j], w[16 + j]), d2by = pk2(w[20 + j], w[20 + j]);
+#pragma unroll
+      for (int e = 0; e < H; e++) {
+        const f32x2 c0 = pk2(c[0][2 * e], c[0][2 * e + 1]), c1 = pk2(c[1][2 * e], c[1][2 * e + 1]);
+        const f32x2 c2 = pk2(c[2][2 * e], c[2][2 * e + 1]), c3 = pk2(c[3][2 * e], c[3][2 * e + 1]);
+        f32x2 z0 = mul2(c0, wz2[0][0]);
+        z0 = fma2(c1, wz2[0][1], z0);
+        z0 = fma2(c2, wz2[0][2], z0);
+        z0 = fma2(c3, wz2[0][3], z0);
+        y[0][e] = fma2(by, z0, y[0][e]);
+        if (VGH) {
+          f32x2 z1 = mul2(c0, wz2[1][0]);
+          z1 = fma2(c1, wz2[1][1], z1);
+          z1 = fma2(c2, wz2[1][2], z1);
+          z1 = fma2(c3, wz2[1][3], z1);
+          f32x2 z2 = mul2(c0, wz2[2][0]);
+          z2 = fma2(c1, wz2[2][1], z2);
+          z2 = fma2(c2, wz2[2][2], z2);
+          z2 = fma2(c3, wz2[2][3], z2);
+          y[1][e] = fma2(dby, z0, y[1][e]);
+          y[2][e] = fma2(d2by, z0, y[2][e]);
+          y[3][e] = fma2(by, z1, y[3][e]);
+          y[4][e] = fma2(dby, z1, y[4][e]);
+          y[5][e] = fma2(by, z2, y[5][e]);
+        }
+      }
+    }
+    const f32x2 ax = pk2(w[i], w[i]), dax = pk2(w[4 + i], w[4 + i]), d2ax = pk2(w[8 + i], w[8 + i]);
+#pragma unroll
+    for (int e = 0; e < H; e++) {
+      // o[q] += x weight * y[r] for the ten (q, weight, r) of the scalar path
+      constexpr int R[10] = {0, 0, 1, 3, 0, 1, 3, 2, 4, 5};
+      constexpr int X[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < (VGH ? 10 : 1); q++) {
+        const f32x2 xw = X[q] == 0 ? ax : (X[q] == 1 ? dax : d2ax);
+        f32x2 acc = pk2(o[q][2 * e], o[q][2 * e + 1]);
+        acc = fma2(xw, y[R[q]][e], acc);
+        upk2(acc, o[q][2 * e], o[q][2 * e + 1]);
+      }
+    }
+    return;
+  }
   A y[6][VW];
 #pragma unroll
   for (int q = 0; q < 6; q++)
