@@ -227,6 +227,43 @@ __device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
   return d;
 }
 
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 neg2(f32x2 a) { return a ^ 0x8000000080000000ull; }
+
+// Two double-float values (one per column) in packed form: the same
+// operations as dfl's, lane by lane.
+struct dfl2 {
+  f32x2 h, l;
+};
+__device__ __forceinline__ dfl2 pk2(dfl a, dfl b) { return dfl2{pk2(a.h, b.h), pk2(a.l, b.l)}; }
+__device__ __forceinline__ void upk2(dfl2 x, dfl &a, dfl &b) {
+  upk2(x.h, a.h, b.h);
+  upk2(x.l, a.l, b.l);
+}
+__device__ __forceinline__ dfl2 mul2(dfl2 a, dfl2 b) {
+  const f32x2 p = mul2(a.h, b.h);
+  f32x2 e = fma2(a.h, b.h, neg2(p));
+  e = fma2(a.h, b.l, e);
+  e = fma2(a.l, b.h, e);
+  return dfl2{p, e};
+}
+__device__ __forceinline__ dfl2 fma2(dfl2 a, dfl2 b, dfl2 c) {
+  const dfl2 p = mul2(a, b);
+  const f32x2 s = add2(c.h, p.h);
+  const f32x2 bb = sub2(s, c.h);
+  const f32x2 t = add2(sub2(c.h, sub2(s, bb)), sub2(p.h, bb));
+  return dfl2{s, add2(t, add2(c.l, p.l))};
+}
+
 // Separable reduction of the 4x4x4 stencil for VW columns.
 // w: [0..11] x weights, [12..23] y weights, [24..35] z weights.
 // o: v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz.
@@ -234,40 +271,41 @@ __device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
 // then this plane's x terms are added to o.
 template <typename A, int VW, bool VGH, typename RowFn>
 __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3][4], RowFn row, A (&o)[10][VW]) {
-  if constexpr (std::is_same<A, float>::value && VW % 2 == 0) {
+  if constexpr ((std::is_same<A, float>::value && VW % 2 == 0) || (std::is_same<A, dfl>::value && VW == 2)) {
     // the same operations on column pairs, two lanes per instruction
+    using P = typename std::conditional<std::is_same<A, float>::value, f32x2, dfl2>::type;
     constexpr int H = VW / 2;
-    f32x2 wz2[3][4];
+    P wz2[3][4];
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
       for (int k = 0; k < 4; k++) wz2[d][k] = pk2(wz[d][k], wz[d][k]);
-    f32x2 y[6][H];
+    P y[6][H];
 #pragma unroll
     for (int q = 0; q < 6; q++)
 #pragma unroll
-      for (int e = 0; e < H; e++) y[q][e] = pk2(0.f, 0.f);
+      for (int e = 0; e < H; e++) y[q][e] = pk2(A(0.f), A(0.f));
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       A c[4][VW];
 #pragma unroll
       for (int k = 0; k < 4; k++) row(j, k, c[k]);
-      const f32x2 by = pk2(w[12 + j], w[12 + j]), dby = pk2(w[16 + j], w[16 + j]), d2by = pk2(w[20 + j], w[20 + j]);
+      const P by = pk2(w[12 + j], w[12 + j]), dby = pk2(w[16 + j], w[16 + j]), d2by = pk2(w[20 + j], w[20 + j]);
 #pragma unroll
       for (int e = 0; e < H; e++) {
-        const f32x2 c0 = pk2(c[0][2 * e], c[0][2 * e + 1]), c1 = pk2(c[1][2 * e], c[1][2 * e + 1]);
-        const f32x2 c2 = pk2(c[2][2 * e], c[2][2 * e + 1]), c3 = pk2(c[3][2 * e], c[3][2 * e + 1]);
-        f32x2 z0 = mul2(c0, wz2[0][0]);
+        const P c0 = pk2(c[0][2 * e], c[0][2 * e + 1]), c1 = pk2(c[1][2 * e], c[1][2 * e + 1]);
+        const P c2 = pk2(c[2][2 * e], c[2][2 * e + 1]), c3 = pk2(c[3][2 * e], c[3][2 * e + 1]);
+        P z0 = mul2(c0, wz2[0][0]);
         z0 = fma2(c1, wz2[0][1], z0);
         z0 = fma2(c2, wz2[0][2], z0);
         z0 = fma2(c3, wz2[0][3], z0);
         y[0][e] = fma2(by, z0, y[0][e]);
         if (VGH) {
-          f32x2 z1 = mul2(c0, wz2[1][0]);
+          P z1 = mul2(c0, wz2[1][0]);
           z1 = fma2(c1, wz2[1][1], z1);
           z1 = fma2(c2, wz2[1][2], z1);
           z1 = fma2(c3, wz2[1][3], z1);
-          f32x2 z2 = mul2(c0, wz2[2][0]);
+          P z2 = mul2(c0, wz2[2][0]);
           z2 = fma2(c1, wz2[2][1], z2);
           z2 = fma2(c2, wz2[2][2], z2);
           z2 = fma2(c3, wz2[2][3], z2);
@@ -279,7 +317,7 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
         }
       }
     }
-    const f32x2 ax = pk2(w[i], w[i]), dax = pk2(w[4 + i], w[4 + i]), d2ax = pk2(w[8 + i], w[8 + i]);
+    const P ax = pk2(w[i], w[i]), dax = pk2(w[4 + i], w[4 + i]), d2ax = pk2(w[8 + i], w[8 + i]);
 #pragma unroll
     for (int e = 0; e < H; e++) {
       // o[q] += x weight * y[r] for the ten (q, weight, r) of the scalar path
@@ -287,8 +325,8 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
       constexpr int X[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
 #pragma unroll
       for (int q = 0; q < (VGH ? 10 : 1); q++) {
-        const f32x2 xw = X[q] == 0 ? ax : (X[q] == 1 ? dax : d2ax);
-        f32x2 acc = pk2(o[q][2 * e], o[q][2 * e + 1]);
+        const P xw = X[q] == 0 ? ax : (X[q] == 1 ? dax : d2ax);
+        P acc = pk2(o[q][2 * e], o[q][2 * e + 1]);
         acc = fma2(xw, y[R[q]][e], acc);
         upk2(acc, o[q][2 * e], o[q][2 * e + 1]);
       }
