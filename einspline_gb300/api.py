@@ -620,6 +620,14 @@ class Determinants:
         self.ainv_ptrs = self._ptrs(ainv)
         self.work = torch.empty(2 * self.nelec * self.W, dtype=torch.float32, device=A.device)
 
+    _CACHE_MAX = 64
+
+    def _remember(self, key, value):
+        if len(self._cache) >= self._CACHE_MAX:
+            self._cache.pop(next(iter(self._cache)))  # oldest entry
+        self._cache[key] = value
+        return value
+
     def _ptrs(self, t):
         """Device array of per-walker pointers into t [W, ...] (cached)."""
         torch = _torch()
@@ -627,7 +635,7 @@ class Determinants:
         if key not in self._cache:
             step = t.stride(0) * t.element_size()
             base = torch.arange(t.shape[0], dtype=torch.int64, device=t.device) * step
-            self._cache[key] = base + t.data_ptr()
+            return self._remember(key, base + t.data_ptr())
         return self._cache[key]
 
     def _index(self, accepted):
@@ -636,7 +644,7 @@ class Determinants:
             return accepted.to(device=self.A.device, dtype=torch.int64)
         key = ("i", tuple(int(i) for i in accepted))
         if key not in self._cache:
-            self._cache[key] = torch.as_tensor(key[1], dtype=torch.int64, device=self.A.device)
+            return self._remember(key, torch.as_tensor(key[1], dtype=torch.int64, device=self.A.device))
         return self._cache[key]
 
     def opts(self, k, pos_f64=False, rule=1):
