@@ -102,3 +102,49 @@ def test_replay_poisson_trace():
     st = S.stats()
     assert st.completed == n and st.released == n
     S.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_concurrent_clients(use_graphs):
+    """Four host threads submit, wait for, check and release uneven requests
+    at once against one server with a tight memory budget (admission must
+    wait for releases); every result equals the direct evaluation bit for
+    bit and the server's counters balance at the end."""
+    import threading
+
+    import torch
+    G = make_spline(N=64, M=16)
+    per_pt = 10 * 64 * 4
+    S = api.Server(G, use_graphs=use_graphs, max_inflight=3, max_batch_points=2048,
+                   hbm_budget_bytes=6 * 512 * per_pt)
+    errors = []
+
+    def client(c):
+        try:
+            rng = np.random.default_rng(700 + c)
+            for r in range(60):
+                n = int(rng.integers(1, 512))
+                pos = synth.points_uniform(800 + 97 * c + r, n)
+                rid = S.submit(pos)
+                S.wait(rid, timeout=60.0)
+                got = S.result(rid, n)
+                S.release(rid)
+                ref = G.eval(torch.from_numpy(pos).cuda(), vgh=True, rule=0, layout=0)
+                for a, b in zip(got, ref):
+                    if not np.array_equal(a, b.cpu().numpy().reshape(a.shape)):
+                        errors.append((c, r))
+                        return
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append((c, repr(e)))
+
+    threads = [threading.Thread(target=client, args=(c,)) for c in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not any(t.is_alive() for t in threads), "a client did not finish"
+    assert not errors, errors[:3]
+    st = S.stats()
+    assert st.submitted == st.completed == st.released == 240
+    S.close()
