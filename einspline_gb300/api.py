@@ -132,8 +132,16 @@ class MultiUBspline3D:
         return a.value, b.value, c.value
 
     def set_load_mode(self, mode: int) -> None:
-        """0 direct loads, 1 L2 bulk prefetch, 2 shared-memory async pipeline, -1 autotuned."""
+        """0 direct loads, 1 L2 bulk prefetch, 2 shared-memory async pipeline,
+        3 the same with 8 columns a thread (16-bit tables), 4 shared-memory
+        pipeline fed by tensor-map (TMA) copies, -1 autotuned."""
         _lib().einspline_gb300_set_load_mode(self.table, int(mode))
+        check()
+
+    def wait_status(self) -> None:
+        """Raises (ETIMEOUT) when a TMA-staged launch on this table gave up a
+        bounded barrier wait since the last check; call after synchronising."""
+        _lib().einspline_gb300_wait_status(self.table)
         check()
 
     def get_load_mode(self) -> int:

@@ -273,15 +273,21 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
   }
   EG_CUDA(cudaStreamSynchronize(t->pipe_stream[0]));
   EG_CUDA(cudaStreamSynchronize(t->pipe_stream[1]));
-  return 0;
+  return wait_status(t, "einspline_gb300_eval_3d_host");
 }
 
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode) {
   clear();
   if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
-  if (mode < -1 || mode > 3) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1, 2 or 3");
+  if (mode < -1 || mode > 4) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1, 2, 3 or 4");
   t->tile_mode = mode;
   return 0;
+}
+
+int einspline_gb300_wait_status(einspline_gb300_table *t) {
+  clear();
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  return wait_status(t, "einspline_gb300_wait_status");
 }
 
 int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb) {
@@ -348,11 +354,20 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
   const int v = vgh ? 1 : 0;
   const int saved_tuned = t->tuned_tx[v];
   t->tuned_tx[v] = 0;
-  const int nmodes = t->storage == ST_F64 ? 2 : (is16(t->storage) ? 4 : 3);
-  for (int pf = 0; pf < nmodes; pf++) {
+  // Load modes worth timing: IEEE FP64 has the direct kernels only, the wide
+  // pipeline (3) is for 16-bit tables.
+  const int ks = t->storage == ST_F64 ? (t->fp64_mode == 1 && t->df_coefs ? (int)ST_DF : (int)ST_F64) : t->storage;
+  std::vector<int> modes = {0, 1};
+  if (ks != ST_F64) {
+    modes.push_back(2);
+    if (is16(ks)) modes.push_back(3);
+    modes.push_back(4);
+  }
+  for (int pf : modes) {
     t->tile_mode = pf;
+    const int vw = VW * ((pf == 3 || (pf == 4 && is16(ks))) ? 2 : 1);
     for (int tx = 32; tx <= 256; tx *= 2) {
-      if (tx > 32 && (tx / 2) * VW >= t->ncol) break;  // wider tiles only idle threads
+      if (tx > 32 && (tx / 2) * vw >= t->ncol) break;  // wider tiles only idle threads
       if (pf == 3 && tx > 32) break;                   // the wide pipeline is one warp per block
       for (int ty = 1; tx * ty <= 256 && (pf < 2 || ty == 1); ty *= 2)
         for (int m = 1; m <= 8; m *= 2) {

@@ -1,6 +1,7 @@
 // Internal declarations shared by the library's translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -130,6 +131,9 @@ struct einspline_gb300_table {
 
   // launch shape and load mode (-1: not forced)
   int tile_tx = 0, tile_ty = 0, tile_pb = 0, tile_mode = -1;
+  // set by a TMA-staged evaluation whose bounded barrier wait ran out
+  // (mapped pinned host word and its device address)
+  int *wait_err_h = nullptr, *wait_err_d = nullptr;
   int tuned_tx[2] = {0, 0}, tuned_ty[2] = {0, 0}, tuned_pb[2] = {0, 0}, tuned_mode[2] = {0, 0};
 };
 
@@ -193,7 +197,8 @@ struct EvalArgs {
   int ntiles;                 // column tiles per point group
   int pb;                     // points per block
   int mode;                   // load mode: 0 direct loads, 1 L2 bulk prefetch first,
-                              // 2/3 shared-memory pipeline of async copies
+                              // 2/3 shared-memory pipeline of async copies,
+                              // 4 shared-memory pipeline of tensor-map (TMA) copies
   int out;                    // 0 vgh; 1 vgl with lattice transform (GPU entries):
                               // 4 rows G.grad and Tr(G^T G H) at lrow apart in gl_pp;
                               // 2 vgl (CPU entries): grads and lapl = trace(H) in hess;
@@ -203,9 +208,17 @@ struct EvalArgs {
                               // as the reference's 1D GPU vgl kernels return them
   const void *linv;           // out 1: 3x3 row-major G (output type)
   int64_t lrow;               // out 1: row stride of the gradient/laplacian rows (reals)
+  int *wait_err;              // mode 4: set to 1 when a bounded barrier wait ran out
+  int box_bytes;              // mode 4: bytes of one box row (<= 256 stored reals)
+  // mode 4: the table as a 4D tensor [x][y][z][column] (column innermost);
+  // CUtensorMap is 128-byte aligned, and so is EvalArgs
+  CUtensorMap tmap;
 };
 
 int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb);
+// ETIMEOUT (and clears the word) when a TMA-staged evaluation on t gave up a
+// bounded wait since the last check; call after the launches completed.
+int wait_status(Table *t, const char *fn);
 // Device and pinned host scratch of the single-point entries (40 * ncol reals).
 int point_scratch(Table *t, const char *fn);
 void fill_eval_geometry(const Table *t, EvalArgs &a);

@@ -351,6 +351,136 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   }
 }
 
+// Tensor-map pipeline: a stage is again one x-plane of one point, but the
+// block's whole 16-row slice of it arrives by one tiled TMA copy per box
+// (a box is <= 256 stored reals wide x 4 z x 4 y x 1 x; a tile wider than
+// that takes several boxes side by side), issued by thread 0 and completing on
+// the stage's full mbarrier.  A box lands row by row, (j*4 + k) * box_bytes
+// apart, which is the row layout the reduction reads.  Each warp releases a
+// stage on its empty mbarrier once its lanes have read it; thread 0 waits
+// for every warp's release before it refills the buffer.  Every thread reads
+// 16 bytes a row: 8 columns of a 16-bit table, 4 FP32 or 2 double-float.
+// Same arithmetic, same order as k_eval.  A wait that runs out sets
+// a.wait_err, leaves the loop on every warp, and thread 0 then waits (again
+// bounded) for the copies it issued before the block exits.
+template <int ST, bool VGH>
+__global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalArgs a) {
+  using A = typename CT<ST>::A;
+  using Raw = typename CT<ST>::Raw;
+  constexpr bool WIDE = is16(ST);
+  constexpr int VW = WIDE ? 2 * CT<ST>::VW : CT<ST>::VW;
+  constexpr int NS = TmaStages<ST>::value;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tile = blockIdx.x % a.ntiles;
+  const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
+  const int nthr = blockDim.x;
+  if (threadIdx.x == 0) tma_prefetch_map(&a.tmap);
+  const int pn = eval_prologue<A>(a, smem, p0, threadIdx.x, nthr);
+  const unsigned base_s = (unsigned)__cvta_generic_to_shared(smem);
+  const unsigned pipe_s = (base_s + (unsigned)smem_total(a.pb, sizeof(A)) + 127u) & ~127u;
+  const unsigned stage_bytes = 256u * (unsigned)nthr;
+  const unsigned full_s = pipe_s + NS * stage_bytes, empty_s = full_s + 8 * NS;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      mbar_init(full_s + 8 * s, 1);
+      mbar_init(empty_s + 8 * s, (unsigned)(nthr >> 5));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const A *sw = reinterpret_cast<const A *>(smem);
+  const int *sidx = reinterpret_cast<const int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
+  const int64_t *ssrc =
+      reinterpret_cast<const int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
+  const unsigned char *pipe = smem + (pipe_s - base_s);
+
+  const int bb = a.box_bytes;
+  const int nbox = (nthr * 16) / bb;
+  const int c_first = tile * nthr * VW;  // first stored real of the block's tile
+  const int box_cols = bb / CT<ST>::BYTES;
+  const int col0 = c_first + threadIdx.x * VW;
+  const bool active = col0 < a.ncol;
+  const unsigned my = (unsigned)((threadIdx.x * 16 / bb) * 16 * bb + (threadIdx.x * 16) % bb);
+  const int S = pn * 4;
+
+  // Thread 0 only: refill the buffer of stage q once every warp has released
+  // its previous stage (q - NS).
+  auto produce = [&](int q) -> bool {
+    const int slot = q % NS;
+    if (q >= NS && !mbar_wait(empty_s + 8 * slot, (unsigned)((q / NS - 1) & 1))) return false;
+    const int pp = q >> 2, i = q & 3;
+    const unsigned full = full_s + 8 * slot;
+    mbar_arrive_expect_tx(full, stage_bytes);
+    for (int b = 0; b < nbox; b++)
+      tma_load_4d(pipe_s + slot * stage_bytes + b * 16 * bb, &a.tmap, full, c_first + b * box_cols,
+                  sidx[3 * pp + 2], sidx[3 * pp + 1], sidx[3 * pp] + i);
+    return true;
+  };
+  int issued = 0;
+  if (threadIdx.x == 0)
+    for (; issued < NS - 1 && issued < S; issued++) produce(issued);
+
+  A o[10][VW];
+  zero_out<A, VW>(o);
+  A wz[3][4];
+  int st = 0;
+  for (; st < S; st++) {
+    bool good = true;
+    if (threadIdx.x == 0 && issued < S) {
+      good = produce(issued);
+      if (good) issued++;
+    }
+    good = mbar_wait(full_s + 8 * (st % NS), (unsigned)((st / NS) & 1)) && good;
+    if (!__all_sync(0xffffffffu, good)) break;
+    const int pp = st >> 2, i = st & 3;
+    const A *w = sw + pp * 36;
+    if (i == 0) z_weights<A>(w, wz);
+    const unsigned char *slot = pipe + (size_t)(st % NS) * stage_bytes + my;
+    reduce_plane<A, VW, VGH>(
+        i, w, wz,
+        [&](int j, int k, A(&c)[VW]) {
+          const Raw *rp = reinterpret_cast<const Raw *>(slot + (j * 4 + k) * bb);
+          if (WIDE) {
+            A lo[CT<ST>::VW], hi[CT<ST>::VW];
+            CT<ST>::decode(rp[0], lo);
+            CT<ST>::decode(rp[1], hi);
+#pragma unroll
+            for (int e = 0; e < CT<ST>::VW; e++) { c[e] = lo[e]; c[CT<ST>::VW + e] = hi[e]; }
+          } else {
+            CT<ST>::decode(rp[0], *reinterpret_cast<A(*)[CT<ST>::VW]>(&c[0]));
+          }
+        },
+        o);
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(empty_s + 8 * (st % NS));
+    if (i == 3) {
+      if (active) {
+        if constexpr (ST == ST_DF) {
+          double od[10][VW];
+#pragma unroll
+          for (int q = 0; q < (VGH ? 10 : 1); q++)
+#pragma unroll
+            for (int e = 0; e < VW; e++) od[q][e] = to_double(o[q][e]);
+          epilogue<double, VW, VGH>(a, ssrc[pp], col0, od);
+        } else {
+          epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
+        }
+      }
+      zero_out<A, VW>(o);
+    }
+  }
+  if (st < S) {
+    // A wait ran out: report it, and let no copy land after the block exits.
+    if ((threadIdx.x & 31) == 0 && a.wait_err) {
+      *(volatile int *)a.wait_err = 1;
+      __threadfence_system();
+    }
+    if (threadIdx.x == 0)
+      for (int q = st; q < issued; q++) mbar_wait(full_s + 8 * (q % NS), (unsigned)((q / NS) & 1));
+  }
+}
+
 // Index of third-derivative entry m (3x3x3 row-major, m = 9a + 3b + c) among
 // the ten distinct ones (xxx, xxy, xxz, xyy, xyz, xzz, yyy, yyz, yzz, zzz).
 __device__ __forceinline__ int g27to10(int m) {
@@ -522,12 +652,14 @@ void fill_eval_geometry(const Table *t, EvalArgs &a) {
 }
 
 // Load modes: 0 direct, 1 L2 prefetch + direct, 2 shared-memory pipeline,
-// 3 shared-memory pipeline with 8 columns per thread (16-bit tables).
+// 3 shared-memory pipeline with 8 columns per thread (16-bit tables),
+// 4 shared-memory pipeline fed by tensor-map (TMA) copies.
 // (IEEE FP64 has only the direct-load kernel; the double-float path has the
-// direct and the 4-column pipelined kernels.)
+// direct, the 4-column pipelined and the TMA kernels.)
 template <int ST, bool VGH>
 static const void *kernel_for(int mode) {
   if constexpr (ST != ST_F64) {
+    if (mode == 4) return (const void *)k_eval_tma<ST, VGH>;
     if (mode == 2 || (mode == 3 && ST == ST_DF)) return (const void *)k_eval_pipe<ST, VGH, false>;
     if constexpr (ST != ST_DF)
       if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
@@ -548,8 +680,59 @@ static int kernel_storage(const Table *t) {
   return (t->storage == ST_F64 && t->fp64_mode == 1 && t->df_coefs) ? (int)ST_DF : t->storage;
 }
 
-// Kernel, block and dynamic shared memory of a launch; the pipelined kernel
-// runs one point lane (ty = 1) and needs its stage buffers raised above the
+// The driver's tensor-map encoder, looked up once through the runtime (no
+// link-time dependence on the driver library).
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiled encoder() {
+  static EncodeTiled fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<EncodeTiled>(p);
+  }();
+  return fn;
+}
+
+// Tensor map of a table's coefficients (base: the stored table or its
+// double-float shadow, es bytes per stored real) as [x][y][z][column], one
+// box = box_cols columns x 4 z x 4 y x 1 x.  Columns past ncol_pad read as
+// zero.  The base is a cudaMalloc address and every stride a multiple of the
+// 128-byte row, so the encoder's 16-byte rules hold.
+static int encode_table_map(const Table *t, const void *base, int es, int box_cols, CUtensorMap *map) {
+  EncodeTiled fn = encoder();
+  if (!fn) return fail(EINSPLINE_GB300_ECUDA, "cuTensorMapEncodeTiled is not available");
+  const cuuint64_t dims[4] = {(cuuint64_t)t->ncol_pad, (cuuint64_t)t->Nc[2], (cuuint64_t)t->Nc[1],
+                              (cuuint64_t)t->Nc[0]};
+  const cuuint64_t strides[3] = {(cuuint64_t)(t->zs * es), (cuuint64_t)(t->ys * es), (cuuint64_t)(t->xs * es)};
+  const cuuint32_t box[4] = {(cuuint32_t)box_cols, 4, 4, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUtensorMapDataType dt =
+      es == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : es == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32 : CU_TENSOR_MAP_DATA_TYPE_UINT64;
+  const CUresult r = fn(map, dt, 4, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(EINSPLINE_GB300_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return 0;
+}
+
+// Largest dynamic shared memory a block may opt into on the current device.
+static size_t max_smem_optin() {
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 227 * 1024;
+  }
+  return (size_t)v;
+}
+
+// Kernel, block and dynamic shared memory of a launch; the pipelined kernels
+// run one point lane (ty = 1) and need their stage buffers raised above the
 // 48 KB default once per kernel.
 static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *block,
                         size_t *smem) {
@@ -560,20 +743,31 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   const int ks = kernel_storage(t);
   if (a.mode >= 2 && ks == ST_F64) a.mode = 0;        // IEEE FP64 is FMA-bound: no pipeline variant
   if (a.mode == 3 && !is16(t->storage)) a.mode = 2;   // the wide variant is for 16-bit tables
-  const int VW = elems_per_thread(t) * (a.mode == 3 ? 2 : 1);
+  const int VW = elems_per_thread(t) * ((a.mode == 3 || (a.mode == 4 && is16(t->storage))) ? 2 : 1);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   *smem = smem_total(pb, acc_bytes(t));
   if (a.mode == 3) {
     tx = 32;  // the wide pipeline runs one warp per block
     a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   }
-  if (a.mode >= 2) {
+  if (ks == ST_DF) a.coefs = t->df_coefs;
+  if (a.mode == 4) {
+    ty = 1;
+    // narrower tiles where the stage buffers would not fit in shared memory
+    const int stages = ks == ST_DF ? TmaStages<ST_DF>::value : kTmaStages;
+    while (tx > 32 && tma_smem(pb, acc_bytes(t), tx, stages) > max_smem_optin()) tx /= 2;
+    a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
+    const int es = is16(t->storage) ? 2 : (ks == ST_F32 ? 4 : 8);
+    a.box_bytes = tx * 16 < 256 * es ? tx * 16 : 256 * es;
+    a.wait_err = t->wait_err_d;
+    if (int r = encode_table_map(t, a.coefs, es, a.box_bytes / es, &a.tmap)) return r;
+    *smem = tma_smem(pb, acc_bytes(t), tx, stages);
+  } else if (a.mode >= 2) {
     ty = 1;
     const int rb = (ks == ST_F32 || ks == ST_DF || a.mode == 3) ? 16 : 8;
     *smem = align_up(*smem, 16) + pipe_bytes(tx, rb, ks == ST_DF ? PipeStages<ST_DF>::value : kPipeStages);
   }
   *block = dim3(tx, ty);
-  if (ks == ST_DF) a.coefs = t->df_coefs;
   switch (ks) {
     case ST_DF: *func = vgh ? kernel_for<ST_DF, true>(a.mode) : kernel_for<ST_DF, false>(a.mode); break;
     case ST_F32: *func = vgh ? kernel_for<ST_F32, true>(a.mode) : kernel_for<ST_F32, false>(a.mode); break;
@@ -660,6 +854,15 @@ void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb) {
   (void)npts;
 }
 
+int wait_status(Table *t, const char *fn) {
+  if (t->wait_err_h && *(volatile int *)t->wait_err_h) {
+    *(volatile int *)t->wait_err_h = 0;
+    return fail(EINSPLINE_GB300_ETIMEOUT, "%s: a TMA-staged evaluation gave up a bounded wait; its results are incomplete",
+                fn);
+  }
+  return 0;
+}
+
 // Device and pinned host scratch for the single-point entries: 40 output
 // reals per column (value, 3 gradient, 9 Hessian, 27 third-derivative).
 int point_scratch(Table *t, const char *fn) {
@@ -725,6 +928,7 @@ void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, 
     cuda_check(cudaGetLastError(), fn);
     return;
   }
+  if (wait_status(t, fn)) return;
   memcpy(vals, t->pt_host, n * rb);
   if (vgh) {
     memcpy(grads, (char *)t->pt_host + n * rb, 3 * n * rb);

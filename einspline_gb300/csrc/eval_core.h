@@ -485,4 +485,73 @@ struct PipeStages { static constexpr int value = kPipeStages; };
 template <>
 struct PipeStages<ST_DF> { static constexpr int value = 2; };
 
+// ------------------------------------------------------------ tensor-map copies
+// Stages of the TMA pipeline and its shared memory: the block's weights and
+// indices, 128-byte alignment slack, the stage buffers (16 rows of 16 bytes
+// a thread) and one full and one empty mbarrier per stage.
+constexpr int kTmaStages = 3;
+// The double-float reduction is arithmetic-bound: two stages and more
+// resident warps, as in its copy pipeline.
+template <int ST>
+struct TmaStages { static constexpr int value = kTmaStages; };
+template <>
+struct TmaStages<ST_DF> { static constexpr int value = 2; };
+__host__ __device__ __forceinline__ size_t tma_smem(int pb, int accb, int nthr, int stages) {
+  return smem_total(pb, accb) + 128 + (size_t)stages * 16 * 16 * nthr + 2 * stages * 8;
+}
+// Longest wait on one mbarrier phase before the kernel gives up: a stage's
+// copy normally lands within microseconds.
+constexpr unsigned long long kWaitNs = 500000000ull;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// Arrives and adds the bytes the phase's copies will deliver.
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// Waits until the phase of the given parity has completed; false when
+// kWaitNs of global time passed first.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  unsigned long long t0 = 0;
+  for (unsigned n = 1;; n++) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((n & 63) == 0) {
+      const unsigned long long now = global_ns();
+      if (n == 64) t0 = now;
+      else if (now - t0 > kWaitNs) return false;
+    }
+  }
+}
+// Brings a tensor map (kernel parameter) into the descriptor cache.
+__device__ __forceinline__ void tma_prefetch_map(const CUtensorMap *map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+// One tiled 4D tensor-map copy into shared memory, completing on mbarrier
+// bar; c0 is the innermost (column) coordinate.
+__device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map, unsigned bar, int c0, int c1,
+                                            int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+
 }  // namespace eg

@@ -453,6 +453,14 @@ Table *table_create(char kind, const GridDesc g[3], int num_splines, int storage
     return nullptr;
   }
   if (alloc_storage(t)) { table_destroy(t); return nullptr; }
+  if (cudaHostAlloc((void **)&t->wait_err_h, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void **)&t->wait_err_d, t->wait_err_h, 0) != cudaSuccess) {
+    cudaGetLastError();
+    fail(EINSPLINE_GB300_ENOMEM, "cannot allocate the wait-status word");
+    table_destroy(t);
+    return nullptr;
+  }
+  *t->wait_err_h = 0;
   // Line factors for the axes, packed into one device buffer.
   std::vector<double> all, one;
   for (int a = 0; a < dims; a++) {
@@ -499,6 +507,7 @@ void table_destroy(Table *t) {
   cudaFree(t->factors_d);
   cudaFree(t->pt_dev);
   if (t->pt_host) cudaFreeHost(t->pt_host);
+  if (t->wait_err_h) cudaFreeHost(t->wait_err_h);
   cudaFree(t->pipe_dev);
   cudaFree(t->sort_dev);
   for (int i = 0; i < 2; i++) {

@@ -28,7 +28,8 @@ def main():
     ap.add_argument("--vgh", type=int, default=1)
     ap.add_argument("--tile", type=int, nargs=3, default=None)
     ap.add_argument("--sort", type=int, default=0)
-    ap.add_argument("--mode", type=int, default=-1, help="load mode: 0 direct, 1 L2 prefetch, 2 smem pipeline")
+    ap.add_argument("--mode", type=int, default=-1, help="load mode: 0 direct, 1 L2 prefetch, 2 smem pipeline, "
+                    "3 wide smem pipeline (16-bit), 4 TMA pipeline")
     ap.add_argument("--sweep", type=int, default=0, help="time every tile shape in every load mode")
     ap.add_argument("--det", type=int, default=0,
                     help="W > 0: time the fused determinant ratio (value, gradient, Laplacian; transposed "
@@ -88,7 +89,7 @@ def main():
     torch.cuda.synchronize()
     if args.sweep:
         res = []
-        for pf in (0, 1, 2, 3):
+        for pf in (0, 1, 2, 3, 4):
             T.set_load_mode(pf)
             for tx in (32, 64, 128, 256):
                 for ty in (1, 2, 4, 8):

@@ -172,11 +172,22 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  *      (FP32 and 16-bit tables; one point lane per block);
  *   3: as 2 with 8 columns and one 16-byte copy per thread and row (16-bit
  *      tables; others use 2);
+ *   4: a three-stage shared-memory pipeline fed by tensor-map (TMA) copies:
+ *      one copy brings the 4x4 stencil rows of a point's x-plane for the
+ *      whole block, completion is tracked by mbarriers; 8 columns a thread
+ *      for 16-bit tables, 4 for FP32, 2 for double-float (IEEE FP64 uses 0);
  *  -1: the autotuned choice; untuned, vgh uses 3 for 16-bit tables and 2
  *      for FP32 (the choices the autotuner makes on GB300), value-only and
  *      FP64 use 0.  Results are identical in all modes. */
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode);
 int einspline_gb300_get_load_mode(einspline_gb300_table *t);
+/* Every wait of the mode-4 kernels on their mbarriers is bounded (0.5 s);
+ * one that runs out makes the block stop early and sets a word that this
+ * call reads and clears: EINSPLINE_GB300_ETIMEOUT when some launch on t since
+ * the last check gave up (its results are incomplete), else 0.  Call it
+ * after the launches have completed (synchronised stream).  The blocking
+ * entries (single-point, host-buffer) check it themselves. */
+int einspline_gb300_wait_status(einspline_gb300_table *t);
 /* Time every candidate tile in every load mode on this table for npts
  * random points and keep the fastest (for vgh when vgh != 0); the choice is
  * cached per table. */
