@@ -367,8 +367,11 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
         raw, _ = tabs["f32"].table_host()
-        cpu_rate, cores, sample = cpu_eval_rate(np.ascontiguousarray(raw), raw.shape[-1], args.cpu_seconds)
-        cpu = {"value": cpu_rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        raw = np.ascontiguousarray(raw)
+        cpu_rate, cores, sample = cpu_eval_rate(raw, raw.shape[-1], args.cpu_seconds)
+        one_rate, _, one_sample = cpu_eval_rate(raw, raw.shape[-1], min(3.0, args.cpu_seconds), nthreads=1)
+        cpu = {"value": cpu_rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+               "single_thread": {"value": one_rate, "cores": 1, "sample": one_sample}}
 
     err = None
     if rank == 0 and args.error_points > 0:
@@ -584,7 +587,8 @@ def other_configs(args):
     """Throughput of the other workloads (parity-test configurations, not
     the headline): FP64 48^3 x 512 plane waves, 128 x 256 points; complex
     64^3 x 256, 256 x 128 points, random vs cell-sorted; FP32/F16
-    128^3 x 2048, chunks of 256 walkers x 256 points."""
+    128^3 x 2048, the 4096 x 256-point step in one launch, random vs
+    cell-sorted."""
     import torch
     from einspline_gb300 import api, synth
     out = {}
@@ -633,19 +637,25 @@ def other_configs(args):
                               "GBps_alg_random": rate(t, p) * 592 / 1e9}
     del t
     out["ld1_s_512_1024"] = lowdim_1d()
+    # The whole 4096-walker step in one launch: 1,048,576 points x 2048
+    # splines, 84 GB of vgh outputs resident in HBM beside the table.
+    P = 4096 * 256
+    p = torch.from_numpy(synth.points_uniform(506, P)).cuda()
+    bufs = (torch.empty((P, 2048), device="cuda"), torch.empty((P, 2048, 3), device="cuda"),
+            torch.empty((P, 2048, 6), device="cuda"))
     for name, st, bpe in (("f32", api.STORE_F32, 296), ("f16", api.STORE_F16, 168)):
         t = dev_table("s", 128, 2048, 505, storage=st)
         t.autotune(16384)
-        P = 256 * 256
-        p = torch.from_numpy(synth.points_uniform(506, P)).cuda()
-        bufs = (torch.empty((P, 2048), device="cuda"), torch.empty((P, 2048, 3), device="cuda"),
-                torch.empty((P, 2048, 6), device="cuda"))
         r = rate(t, p, reps=3, out_bufs=bufs)
-        out[f"s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9,
-                                            "note": "256 walkers x 256 points per launch (the 4096-walker step "
-                                                    "is 16 such launches; outputs of all 4096 would be 84 GB)"}
-        del t, bufs
+        rs = rate(t, p, reps=3, sort=True, out_bufs=bufs)
+        out[f"s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9, "sorted_evals_per_s": rs,
+                                            "note": "4096 walkers x 256 points in one launch (84 GB of outputs); "
+                                                    "sorted: the step's points visited in Morton order of their "
+                                                    "cells, sort kernels timed"}
+        del t
         torch.cuda.empty_cache()
+    del bufs, p
+    torch.cuda.empty_cache()
     return out
 
 
