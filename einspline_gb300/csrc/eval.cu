@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   using Raw = typename CT<ST>::Raw;
   constexpr int VW = WIDE ? 2 * CT<ST>::VW : CT<ST>::VW;
   constexpr int RB = WIDE ? 2 * (int)sizeof(Raw) : (int)sizeof(Raw);
-  constexpr int NS = PipeStages<ST>::value;
+  constexpr int NS = pipe_stages(ST, WIDE);
   extern __shared__ __align__(16) unsigned char smem[];
   const int tile = blockIdx.x % a.ntiles;
   const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
@@ -765,7 +765,7 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   } else if (a.mode >= 2) {
     ty = 1;
     const int rb = (ks == ST_F32 || ks == ST_DF || a.mode == 3) ? 16 : 8;
-    *smem = align_up(*smem, 16) + pipe_bytes(tx, rb, ks == ST_DF ? PipeStages<ST_DF>::value : kPipeStages);
+    *smem = align_up(*smem, 16) + pipe_bytes(tx, rb, pipe_stages(ks, a.mode == 3 && is16(ks)));
   }
   *block = dim3(tx, ty);
   switch (ks) {
