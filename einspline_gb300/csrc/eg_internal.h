@@ -61,6 +61,7 @@ void build_line_factors(int M, int lcode, int rcode, double delta_inv, LineFacto
 struct PackedFactors {
   int M, cyclic, anti, pad_;
   double F, Q, R0, R1, U0a, U0b;
+  double QH, QL;  // Q's reciprocal as hi + lo (QH = 0: divide Q directly)
 };
 size_t packed_factor_doubles(int M);
 void pack_line_factors(const LineFactors &f, std::vector<double> &out);

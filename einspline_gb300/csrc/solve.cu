@@ -13,6 +13,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <math.h>
+
+#include <cmath>
 #include <stdio.h>
 #include <string.h>
 
@@ -118,7 +120,17 @@ void build_line_factors(int M, int lcode, int rcode, double dinv, LineFactors &f
   }
 }
 
-size_t packed_factor_doubles(int M) { return sizeof(PackedFactors) / sizeof(double) + 5 * (size_t)(M + 2); }
+size_t packed_factor_doubles(int M) { return sizeof(PackedFactors) / sizeof(double) + 7 * (size_t)(M + 2); }
+
+// A divisor's reciprocal as hi + lo: hi = RN(1/b), lo = RN((1 - b*hi)/b)
+// (1 - b*hi is exact by FMA).  hi = lo = 0 marks a divisor outside
+// [2^-64, 2^64] (or zero), which the device divides directly.
+static void split_reciprocal(double b, double &hi, double &lo) {
+  const double a = std::fabs(b);
+  if (!(a >= 0x1p-64 && a <= 0x1p64)) { hi = lo = 0.0; return; }
+  hi = 1.0 / b;
+  lo = std::fma(-b, hi, 1.0) / b;
+}
 
 void pack_line_factors(const LineFactors &f, std::vector<double> &out) {
   const int n = f.M + 2;
@@ -127,6 +139,7 @@ void pack_line_factors(const LineFactors &f, std::vector<double> &out) {
   memset(&h, 0, sizeof(h));
   h.M = f.M; h.cyclic = f.cyclic; h.anti = f.anti;
   h.F = f.F; h.Q = f.Q; h.R0 = f.R0; h.R1 = f.R1; h.U0a = f.U0a; h.U0b = f.U0b;
+  split_reciprocal(f.Q, h.QH, h.QL);
   memcpy(out.data(), &h, sizeof(h));
   double *p = out.data() + sizeof(PackedFactors) / sizeof(double);
   std::copy(f.P.begin(), f.P.end(), p + 0 * n);
@@ -134,6 +147,7 @@ void pack_line_factors(const LineFactors &f, std::vector<double> &out) {
   std::copy(f.E.begin(), f.E.end(), p + 2 * n);
   std::copy(f.U.begin(), f.U.end(), p + 3 * n);
   std::copy(f.LC.begin(), f.LC.end(), p + 4 * n);
+  for (size_t i = 0; i < f.P.size(); i++) split_reciprocal(f.P[i], p[5 * n + i], p[6 * n + i]);
 }
 
 // ------------------------------------------------------------------
@@ -153,10 +167,26 @@ __host__ __device__ __forceinline__ double dsub(double a, double b) {
   return a - b;
 #endif
 }
-__host__ __device__ __forceinline__ double ddiv(double a, double b) {
+// a / b correctly rounded, b a band divisor known in advance with its
+// reciprocal split as zh + zl (split_reciprocal).  On the device:
+// q0 = a*zh + a*zl is within one ulp of a/b, the remainder r = a - b*q0 is
+// exact by FMA, and RN(q0 + r*zh) is the correctly rounded quotient
+// (Markstein's correction step: P. Markstein, IBM J. Res. Dev. 34(1), 1990;
+// the reciprocal known in advance as in N. Brisebarre, J.-M. Muller and
+// S. K. Raina, IEEE Trans. Computers 53(8), 2004): four FP64 operations
+// instead of a full division, the same bits.  Numerators outside
+// [2^-823, 2^825) in magnitude (zeros, subnormals, near overflow) and
+// divisors without a split take the IEEE division, so every intermediate
+// stays normal.  The host divides directly.
+__host__ __device__ __forceinline__ double ddiv(double a, double b, double zh, double zl) {
 #ifdef __CUDA_ARCH__
-  return __ddiv_rn(a, b);
+  const unsigned ea = ((unsigned)__double2hiint(a) >> 20) & 0x7FFu;
+  if (ea < 200u || ea > 1847u || __double2hiint(zh) == 0) return __ddiv_rn(a, b);
+  const double q0 = __fma_rn(a, zh, __dmul_rn(a, zl));
+  const double r = __fma_rn(-q0, b, a);
+  return __fma_rn(r, zh, q0);
 #else
+  (void)zh; (void)zl;
   return a / b;
 #endif
 }
@@ -169,24 +199,24 @@ __host__ __device__ inline void solve_line(const double *pk, const double *in, i
   const PackedFactors &h = *reinterpret_cast<const PackedFactors *>(pk);
   const int M = h.M, n = M + 2;
   const double *P = pk + sizeof(PackedFactors) / sizeof(double);
-  const double *L = P + n, *E = P + 2 * n, *U = P + 3 * n, *LC = P + 4 * n;
+  const double *L = P + n, *E = P + 2 * n, *U = P + 3 * n, *LC = P + 4 * n, *RH = P + 5 * n, *RL = P + 6 * n;
   if (h.cyclic) {
     double dl = in[(int64_t)(M - 1) * is];
     double nxt = in[1 * is];
-    double d = ddiv(in[0], P[0]);
+    double d = ddiv(in[0], P[0], RH[0], RL[0]);
     dl = dsub(dl, dmul(E[0], d));
     out[1 * os] = d;
     double prev = d;
     for (int r = 1; r < M - 1; r++) {
       double cur = nxt;
       nxt = in[(int64_t)(r + 1) * is];
-      d = ddiv(dsub(cur, dmul(L[r], prev)), P[r]);
+      d = ddiv(dsub(cur, dmul(L[r], prev)), P[r], RH[r], RL[r]);
       out[(int64_t)(r + 1) * os] = d;
       if (r < M - 2) dl = dsub(dl, dmul(E[r], d));
       prev = d;
     }
     dl = dsub(dl, dmul(h.F, prev));
-    dl = ddiv(dl, h.Q);
+    dl = ddiv(dl, h.Q, h.QH, h.QL);
     const double cM = dl;
     out[(int64_t)M * os] = cM;
     double cn = cM, c1 = 0.0, c2 = 0.0;
@@ -209,14 +239,14 @@ __host__ __device__ inline void solve_line(const double *pk, const double *in, i
     }
   } else {
     double nxt = in[0];
-    double d0 = ddiv(lval, P[0]);
+    double d0 = ddiv(lval, P[0], RH[0], RL[0]);
     out[0] = d0;
     double prev = d0, prev2 = 0.0;
     for (int r = 1; r <= M; r++) {
       double cur = nxt;
       if (r <= M - 1) nxt = in[(int64_t)r * is];
-      double d = (r == 1) ? ddiv(dsub(cur, dmul(L[1], d0)), P[1])
-                          : ddiv(dsub(cur, dmul(L[r], prev)), P[r]);
+      double d = (r == 1) ? ddiv(dsub(cur, dmul(L[1], d0)), P[1], RH[1], RL[1])
+                          : ddiv(dsub(cur, dmul(L[r], prev)), P[r], RH[r], RL[r]);
       out[(int64_t)r * os] = d;
       prev2 = prev;
       prev = d;
@@ -224,7 +254,7 @@ __host__ __device__ inline void solve_line(const double *pk, const double *in, i
     // prev = d_M, prev2 = d_{M-1}
     double dm1 = dsub(rval, dmul(h.R0, prev2));
     dm1 = dsub(dm1, dmul(h.R1, prev));
-    dm1 = ddiv(dm1, h.Q);
+    dm1 = ddiv(dm1, h.Q, h.QH, h.QL);
     out[(int64_t)(M + 1) * os] = dm1;
     double cn = dm1;
     for (int r = M; r > 0; r--) {

@@ -48,6 +48,28 @@ def test_table_matches_oracle(orc, kind, name, grids, bcs):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("kind", "dz")
+@pytest.mark.parametrize("name,grids,bcs", CASES, ids=[c[0] for c in CASES])
+def test_table_bit_identical_across_magnitudes(orc, kind, name, grids, bcs):
+    """Data from 2^-1000 to 2^900 in magnitude with exact zeros and negative
+    zeros: the device divides by the band divisors through their split
+    reciprocals (Markstein's correction) inside an exponent window and by
+    the IEEE division outside it; the tables keep the reference's bits,
+    signed zeros included."""
+    M = tuple(g[2] for g in grids)
+    N = 9
+    rng = np.random.default_rng(121)
+    base = synth.grid_data_uniform(122, M, N, np.float64, complex_=kind == "z")
+    data = np.ldexp(base, rng.integers(-1000, 900, size=base.shape))
+    flat = data.reshape(-1)
+    flat[rng.choice(flat.size, flat.size // 20, replace=False)] = 0.0
+    flat[rng.choice(flat.size, flat.size // 20, replace=False)] = -0.0
+    G, T, _ = build_pair(orc, kind, grids, bcs, N, data=data)
+    got = np.ascontiguousarray(gpu_table(G))
+    assert np.array_equal(got.view(np.uint64), np.ascontiguousarray(T.coefs64).view(np.uint64))
+
+
+@pytest.mark.gpu
 def test_padding_and_unset_columns_are_zero(orc):
     grids, bcs = CASES[0][1], CASES[0][2]
     G = api.MultiUBspline3D("s", grids, bcs, 5)
