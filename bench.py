@@ -259,6 +259,7 @@ def run_gpu(args):
     def tune(t):
         if args.autotune:
             t.autotune(int(np.mean(npts)), True)
+            t.autotune(int(np.mean(npts)), True, sorted=True)
 
     for t in tabs.values():
         tune(t)
@@ -632,6 +633,7 @@ def other_configs(args):
     del t
     t = dev_table("c", 64, 256, 303)
     t.autotune(256 * 128)
+    t.autotune(256 * 128, sorted=True)
     p = torch.from_numpy(synth.points_uniform(304, 256 * 128)).cuda()
     out["c_64cube_256"] = {"random_evals_per_s": rate(t, p), "sorted_evals_per_s": rate(t, p, sort=True),
                               "GBps_alg_random": rate(t, p) * 592 / 1e9}
@@ -646,6 +648,7 @@ def other_configs(args):
     for name, st, bpe in (("f32", api.STORE_F32, 296), ("f16", api.STORE_F16, 168)):
         t = dev_table("s", 128, 2048, 505, storage=st)
         t.autotune(16384)
+        t.autotune(P, sorted=True)
         r = rate(t, p, reps=3, out_bufs=bufs)
         rs = rate(t, p, reps=3, sort=True, out_bufs=bufs)
         out[f"s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9, "sorted_evals_per_s": rs,

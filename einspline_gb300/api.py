@@ -149,8 +149,12 @@ class MultiUBspline3D:
         check()
         return int(r)
 
-    def autotune(self, npts: int, vgh: bool = True):
-        _lib().einspline_gb300_autotune(self.table, npts, int(vgh))
+    def autotune(self, npts: int, vgh: bool = True, sorted: bool = False):
+        """Time every tile and load mode for batches of npts random points
+        (sorted: for cell-sorted launches of such batches) and keep the
+        fastest; returns the random-order tile."""
+        fn = _lib().einspline_gb300_autotune_sorted if sorted else _lib().einspline_gb300_autotune
+        fn(self.table, npts, int(vgh))
         check()
         return self.get_tile()
 

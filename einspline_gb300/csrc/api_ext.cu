@@ -126,7 +126,7 @@ static int eval_device(Table *t, const einspline_gb300_eval_opts *o, int64_t npt
     a.perm = perm;
   }
   int tx, ty, pb;
-  pick_tile(t, o->vgh != 0, npts, tx, ty, pb);
+  pick_tile(t, o->vgh != 0, npts, tx, ty, pb, a.perm != nullptr);
   return launch_eval(t, a, o->vgh != 0, s, tx, ty, pb);
 }
 
@@ -175,7 +175,10 @@ int einspline_gb300_set_fp64_mode(einspline_gb300_table *t, int mode) {
     t->fp64_mode = mode;
     t->df_stale = true;
     // the kernels differ between the modes: forget the tuned launch shapes
-    for (int v = 0; v < 2; v++) t->tuned_tx[v] = t->tuned_ty[v] = t->tuned_pb[v] = t->tuned_mode[v] = 0;
+    for (int v = 0; v < 2; v++) {
+      t->tuned_tx[v] = t->tuned_ty[v] = t->tuned_pb[v] = t->tuned_mode[v] = 0;
+      t->tuned_s_tx[v] = t->tuned_s_ty[v] = t->tuned_s_pb[v] = t->tuned_s_mode[v] = 0;
+    }
     if (mode == 0) {
       cudaFree(t->df_coefs);  // synchronises the device: no launch still reads it
       t->df_coefs = nullptr;
@@ -313,6 +316,108 @@ int einspline_gb300_get_load_mode(einspline_gb300_table *t) {
   return pick_mode(t, true);
 }
 
+}  // extern "C"
+
+namespace eg {
+
+__global__ void k_gather_pos(const double *pos, const int *perm, int64_t n, double *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t s = perm[i];
+  out[3 * i] = pos[3 * s];
+  out[3 * i + 1] = pos[3 * s + 1];
+  out[3 * i + 2] = pos[3 * s + 2];
+}
+
+// npts points uniform in the table's box (rule 1 measures positions from the
+// grid origin), double, into pos.
+static void uniform_points(Table *t, double *pos, int64_t npts) {
+  einspline_gb300_fill_uniform(pos, 3 * npts, 1, 0x5eed5eedull, 0, 0.0, 1.0, t->stream);
+  k_scale_box<<<(unsigned)((npts + 255) / 256), 256, 0, t->stream>>>(pos, npts, t->end[0] - t->start[0],
+                                                                     t->end[1] - t->start[1], t->end[2] - t->start[2]);
+  count_launch();
+}
+
+// A launch over npts points at pos (double, rule 1, GPU layout) writing to
+// out (room for npts points' outputs).
+static EvalArgs tuning_args(Table *t, const double *pos, int64_t npts, void *out) {
+  const size_t rb = t->storage == ST_F64 ? 8 : 4;
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  fill_eval_geometry(t, a);
+  a.pos = pos;
+  a.pos_f64 = 1;
+  a.rule = 1;
+  a.layout = 0;
+  a.npts = npts;
+  a.vals = out;
+  a.grads = (char *)out + (size_t)npts * t->ncol * rb;
+  a.hess = (char *)out + (size_t)npts * 4 * t->ncol * rb;
+  a.vstride = t->ncol; a.gstride = 3 * (int64_t)t->ncol; a.hstride = 6 * (int64_t)t->ncol;
+  return a;
+}
+
+// Times every load mode and tile shape on launch a (three launches each,
+// after one warm launch) and returns the fastest as {tx, ty, pb, mode}.
+static int tune_shapes(Table *t, const EvalArgs &a, bool vgh, int best_shape[4]) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  const int VW = elems_per_thread(t);
+  const int saved_pf = t->tile_mode;
+  // Load modes worth timing: IEEE FP64 has the direct kernels only, the wide
+  // pipeline (3) is for 16-bit tables.
+  const int ks = t->storage == ST_F64 ? (t->fp64_mode == 1 && t->df_coefs ? (int)ST_DF : (int)ST_F64) : t->storage;
+  std::vector<int> modes = {0, 1};
+  if (ks != ST_F64) {
+    modes.push_back(2);
+    if (is16(ks)) modes.push_back(3);
+    modes.push_back(4);
+  }
+  int rc = 0;
+  for (int pf : modes) {
+    t->tile_mode = pf;
+    const int vw = VW * ((pf == 3 || (pf == 4 && is16(ks))) ? 2 : 1);
+    for (int tx = 32; tx <= 256 && !rc; tx *= 2) {
+      if (tx > 32 && (tx / 2) * vw >= t->ncol) break;  // wider tiles only idle threads
+      if (pf == 3 && tx > 32) break;                   // the wide pipeline is one warp per block
+      for (int ty = 1; tx * ty <= 256 && (pf < 2 || ty == 1) && !rc; ty *= 2)
+        for (int m = 1; m <= 8 && !rc; m *= 2) {
+          const int pb = ty * m;
+          if (pb > 64) continue;
+          EvalArgs b = a;
+          if ((rc = launch_eval(t, b, vgh, t->stream, tx, ty, pb))) break;
+          cudaEventRecord(e0, t->stream);
+          for (int r = 0; r < 3; r++) {
+            b = a;
+            launch_eval(t, b, vgh, t->stream, tx, ty, pb);
+          }
+          cudaEventRecord(e1, t->stream);
+          cudaEventSynchronize(e1);
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (ms < best) {
+            best = ms;
+            best_shape[0] = tx; best_shape[1] = ty; best_shape[2] = pb; best_shape[3] = pf;
+          }
+        }
+    }
+    if (rc) break;
+  }
+  t->tile_mode = saved_pf;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(t->stream);
+  if (e != cudaSuccess) return cuda_check(e, "autotune");
+  return 0;
+}
+
+}  // namespace eg
+
+extern "C" {
+
 int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
   clear();
   if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
@@ -326,81 +431,52 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh) {
     return fail(EINSPLINE_GB300_ENOMEM, "autotune scratch");
   }
   double *pos = (double *)((char *)buf + out_b);
-  // Points uniform in the box: unit draws, scaled per axis by the cell rule
-  // below (rule 1 measures positions from the grid origin).
-  einspline_gb300_fill_uniform(pos, 3 * npts, 1, 0x5eed5eedull, 0, 0.0, 1.0, t->stream);
-  k_scale_box<<<(unsigned)((npts + 255) / 256), 256, 0, t->stream>>>(pos, npts, t->end[0] - t->start[0],
-                                                                     t->end[1] - t->start[1], t->end[2] - t->start[2]);
-  count_launch();
-  EvalArgs a;
-  memset(&a, 0, sizeof(a));
-  fill_eval_geometry(t, a);
-  a.pos = pos;
-  a.pos_f64 = 1;
-  a.rule = 1;
-  a.layout = 0;
-  a.npts = npts;
-  a.vals = buf;
-  a.grads = (char *)buf + (size_t)npts * t->ncol * rb;
-  a.hess = (char *)buf + (size_t)npts * 4 * t->ncol * rb;
-  a.vstride = t->ncol; a.gstride = 3 * (int64_t)t->ncol; a.hstride = 6 * (int64_t)t->ncol;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  float best = 1e30f;
-  int btx = 0, bty = 0, bpb = 0, bpf = 0;
-  const int VW = elems_per_thread(t);
-  const int saved_pf = t->tile_mode;
+  uniform_points(t, pos, npts);
+  const EvalArgs a = tuning_args(t, pos, npts, buf);
+  int shape[4] = {0, 0, 0, 0};
+  const int r = tune_shapes(t, a, vgh != 0, shape);
+  cudaFree(buf);
+  if (r) return r;
   const int v = vgh ? 1 : 0;
-  const int saved_tuned = t->tuned_tx[v];
-  t->tuned_tx[v] = 0;
-  // Load modes worth timing: IEEE FP64 has the direct kernels only, the wide
-  // pipeline (3) is for 16-bit tables.
-  const int ks = t->storage == ST_F64 ? (t->fp64_mode == 1 && t->df_coefs ? (int)ST_DF : (int)ST_F64) : t->storage;
-  std::vector<int> modes = {0, 1};
-  if (ks != ST_F64) {
-    modes.push_back(2);
-    if (is16(ks)) modes.push_back(3);
-    modes.push_back(4);
+  t->tuned_tx[v] = shape[0]; t->tuned_ty[v] = shape[1]; t->tuned_pb[v] = shape[2]; t->tuned_mode[v] = shape[3];
+  return 0;
+}
+
+int einspline_gb300_autotune_sorted(einspline_gb300_table *t, int64_t npts, int vgh) {
+  clear();
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (npts < 1 || npts > INT_MAX) return fail(EINSPLINE_GB300_EINVAL, "npts must be in [1, %d]", INT_MAX);
+  if (int r = table_flush(t)) return r;
+  // The batch's points in cell order; shapes are timed on a window of
+  // consecutive sorted points, which has the batch's local density.
+  const int64_t W = std::min<int64_t>(npts, 32768);
+  const size_t rb = t->storage == ST_F64 ? 8 : 4;
+  const size_t out_b = align_up_sz((size_t)W * t->ncol * rb * (vgh ? 10 : 1), 256);
+  void *buf = nullptr;
+  if (cudaMalloc(&buf, out_b + align_up_sz((size_t)npts * 24, 256) + (size_t)W * 24) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(EINSPLINE_GB300_ENOMEM, "autotune scratch");
   }
-  for (int pf : modes) {
-    t->tile_mode = pf;
-    const int vw = VW * ((pf == 3 || (pf == 4 && is16(ks))) ? 2 : 1);
-    for (int tx = 32; tx <= 256; tx *= 2) {
-      if (tx > 32 && (tx / 2) * vw >= t->ncol) break;  // wider tiles only idle threads
-      if (pf == 3 && tx > 32) break;                   // the wide pipeline is one warp per block
-      for (int ty = 1; tx * ty <= 256 && (pf < 2 || ty == 1); ty *= 2)
-        for (int m = 1; m <= 8; m *= 2) {
-          const int pb = ty * m;
-          if (pb > 64) continue;
-          EvalArgs b = a;
-          if (launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb)) {
-            t->tile_mode = saved_pf;
-            t->tuned_tx[v] = saved_tuned;
-            cudaFree(buf);
-            return einspline_gb300_last_error();
-          }
-          cudaEventRecord(e0, t->stream);
-          for (int r = 0; r < 3; r++) {
-            b = a;
-            launch_eval(t, b, vgh != 0, t->stream, tx, ty, pb);
-          }
-          cudaEventRecord(e1, t->stream);
-          cudaEventSynchronize(e1);
-          float ms = 0;
-          cudaEventElapsedTime(&ms, e0, e1);
-          if (ms < best) { best = ms; btx = tx; bty = ty; bpb = pb; bpf = pf; }
-        }
+  double *all = (double *)((char *)buf + out_b);
+  double *win = (double *)((char *)all + align_up_sz((size_t)npts * 24, 256));
+  uniform_points(t, all, npts);
+  EvalArgs s = tuning_args(t, all, npts, buf);
+  int *perm = nullptr;
+  int r = sort_points(t, s, &perm, t->stream);
+  if (!r) {
+    k_gather_pos<<<(unsigned)((W + 255) / 256), 256, 0, t->stream>>>(all, perm, W, win);
+    count_launch();
+    const EvalArgs a = tuning_args(t, win, W, buf);
+    int shape[4] = {0, 0, 0, 0};
+    r = tune_shapes(t, a, vgh != 0, shape);
+    if (!r) {
+      const int v = vgh ? 1 : 0;
+      t->tuned_s_tx[v] = shape[0]; t->tuned_s_ty[v] = shape[1]; t->tuned_s_pb[v] = shape[2];
+      t->tuned_s_mode[v] = shape[3];
     }
   }
-  t->tile_mode = saved_pf;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaError_t e = cudaStreamSynchronize(t->stream);
   cudaFree(buf);
-  if (e != cudaSuccess) return cuda_check(e, "autotune");
-  t->tuned_tx[v] = btx; t->tuned_ty[v] = bty; t->tuned_pb[v] = bpb; t->tuned_mode[v] = bpf;
-  return 0;
+  return r;
 }
 
 }  // extern "C"

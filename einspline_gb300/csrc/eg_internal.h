@@ -136,6 +136,8 @@ struct einspline_gb300_table {
   // (mapped pinned host word and its device address)
   int *wait_err_h = nullptr, *wait_err_d = nullptr;
   int tuned_tx[2] = {0, 0}, tuned_ty[2] = {0, 0}, tuned_pb[2] = {0, 0}, tuned_mode[2] = {0, 0};
+  // the same for launches that visit points in cell order (sorted batches)
+  int tuned_s_tx[2] = {0, 0}, tuned_s_ty[2] = {0, 0}, tuned_s_pb[2] = {0, 0}, tuned_s_mode[2] = {0, 0};
 };
 
 namespace eg {
@@ -227,9 +229,11 @@ void fill_eval_geometry(const Table *t, EvalArgs &a);
 // (for graph kernel nodes); fills a.pb and a.ntiles.
 int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *grid,
                  dim3 *block, size_t *smem);
-void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb);
+// sorted: the launch visits its points in cell order (a visiting order is
+// set), which has its own tuned shape.
+void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb, bool sorted = false);
 // Load mode of launches on this table (see EvalArgs::mode).
-int pick_mode(Table *t, bool vgh);
+int pick_mode(Table *t, bool vgh, bool sorted = false);
 int elems_per_thread(const Table *t);
 
 // sorting

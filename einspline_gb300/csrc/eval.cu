@@ -739,7 +739,7 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
     return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
   a.pb = pb;
-  a.mode = pick_mode(t, vgh);
+  a.mode = pick_mode(t, vgh, a.perm != nullptr);
   const int ks = kernel_storage(t);
   if (a.mode >= 2 && ks == ST_F64) a.mode = 0;        // IEEE FP64 is FMA-bound: no pipeline variant
   if (a.mode == 3 && !is16(t->storage)) a.mode = 2;   // the wide variant is for 16-bit tables
@@ -824,17 +824,19 @@ int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const 
 // 1024 and 128^3 x 2048 (and 48^3 x 512 double-float): the shared-memory
 // copy pipeline, 8-column wide for 16-bit tables; IEEE FP64 (FMA-bound) and
 // value-only evaluation use direct loads.
-int pick_mode(Table *t, bool vgh) {
+int pick_mode(Table *t, bool vgh, bool sorted) {
   if (t->tile_mode >= 0) return t->tile_mode;
   const int v = vgh ? 1 : 0;
+  if (sorted && t->tuned_s_tx[v]) return t->tuned_s_mode[v];
   if (t->tuned_tx[v]) return t->tuned_mode[v];
   if (vgh && kernel_storage(t) != ST_F64) return is16(t->storage) ? 3 : 2;
   return 0;
 }
 
-void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb) {
+void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb, bool sorted) {
   if (t->tile_tx) { tx = t->tile_tx; ty = t->tile_ty; pb = t->tile_pb; return; }
   const int v = vgh ? 1 : 0;
+  if (sorted && t->tuned_s_tx[v]) { tx = t->tuned_s_tx[v]; ty = t->tuned_s_ty[v]; pb = t->tuned_s_pb[v]; return; }
   if (t->tuned_tx[v]) { tx = t->tuned_tx[v]; ty = t->tuned_ty[v]; pb = t->tuned_pb[v]; return; }
   const int VW = elems_per_thread(t);
   const int need = (t->ncol + VW - 1) / VW;

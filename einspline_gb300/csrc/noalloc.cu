@@ -121,6 +121,6 @@ extern "C" int einspline_gb300_eval_3d_sorted_noalloc(einspline_gb300_table *t, 
   count_launch();
   a.perm = v_out;
   int tx, ty, pb;
-  pick_tile(t, o->vgh != 0, npts, tx, ty, pb);
+  pick_tile(t, o->vgh != 0, npts, tx, ty, pb, true);
   return launch_eval(t, a, o->vgh != 0, s, tx, ty, pb);
 }

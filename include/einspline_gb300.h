@@ -192,6 +192,13 @@ int einspline_gb300_wait_status(einspline_gb300_table *t);
  * random points and keep the fastest (for vgh when vgh != 0); the choice is
  * cached per table. */
 int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh);
+/* The same for launches that visit their points in cell order (opts.sort,
+ * the allocation-free sorted entry): npts random points are sorted by cell
+ * and the shapes are timed on a window of up to 32,768 consecutive sorted
+ * points, so a batch's density (npts per grid cell) is what is tuned for.
+ * Sorted launches then use this choice; set_tile / set_load_mode still
+ * override both; get_tile and get_load_mode report the random-order one. */
+int einspline_gb300_autotune_sorted(einspline_gb300_table *t, int64_t npts, int vgh);
 
 /* --------------------------------------------------------------- serving */
 /* A request server over one table: QMC-walker-shaped requests (a set of

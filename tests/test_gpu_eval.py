@@ -185,3 +185,26 @@ def test_unaligned_strided_outputs(orc):
            h[:, :6 * N].cpu().numpy().reshape(33, N, 6))
     assert_close(got, ref, TOL["s"], "strided")
     assert (v[:, N:] == -7).all() and (g[:, 3 * N:] == -7).all() and (h[:, 6 * N:] == -7).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16])
+def test_sorted_tuning_changes_no_result(orc, storage):
+    """A shape tuned for cell-sorted launches is used by them only; results
+    stay bit-identical to the random-order launch, and the random-order
+    choice is untouched."""
+    G, T, _ = build_pair(orc, "s", PERIODIC_UNIT, [(P, P)] * 3, 40, seed=131, storage=storage)
+    pos = synth.points_uniform(132, 3000, (0, 0, 0), (1, 1, 1))
+    pt = torch_pos(pos)
+    base = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
+    tile0, mode0 = G.get_tile(), G.get_load_mode()
+    G.autotune(3000, sorted=True)
+    assert G.get_tile() == tile0 and G.get_load_mode() == mode0
+    for sort in (True, False):
+        got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0, sort=sort)]
+        for a, b in zip(got, base):
+            assert np.array_equal(a, b), sort
+    G.autotune(3000)
+    got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0, sort=True)]
+    for a, b in zip(got, base):
+        assert np.array_equal(a, b)
