@@ -263,7 +263,8 @@ def run_gpu(args):
 
     for t in tabs.values():
         tune(t)
-    tiles = {k: {"tile": list(t.get_tile()), "load_mode": t.get_load_mode()} for k, t in tabs.items()}
+    tiles = {k: {"tile": list(t.get_tile()), "load_mode": t.get_load_mode(),
+                 "sorted_tile_and_mode": list(t.launch_shape(sorted=True))} for k, t in tabs.items()}
 
     def timed(t, sort=False):
         for k in range(args.warmup):
@@ -652,6 +653,8 @@ def other_configs(args):
         r = rate(t, p, reps=3, out_bufs=bufs)
         rs = rate(t, p, reps=3, sort=True, out_bufs=bufs)
         out[f"s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9, "sorted_evals_per_s": rs,
+                                            "tile_and_mode": list(t.launch_shape()),
+                                            "sorted_tile_and_mode": list(t.launch_shape(sorted=True)),
                                             "note": "4096 walkers x 256 points in one launch (84 GB of outputs); "
                                                     "sorted: the step's points visited in Morton order of their "
                                                     "cells, sort kernels timed"}

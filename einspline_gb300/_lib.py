@@ -208,6 +208,7 @@ def _signatures():
     sig["einspline_gb300_get_tile"] = ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32)
     sig["einspline_gb300_autotune"] = ([vp, i64, i32], i32)
     sig["einspline_gb300_autotune_sorted"] = ([vp, i64, i32], i32)
+    sig["einspline_gb300_get_launch_shape"] = ([vp, i32, i32] + [C.POINTER(i32)] * 4, i32)
     sig["einspline_gb300_set_load_mode"] = ([vp, i32], i32)
     sig["einspline_gb300_get_load_mode"] = ([vp], i32)
     sig["einspline_gb300_wait_status"] = ([vp], i32)

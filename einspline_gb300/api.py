@@ -144,6 +144,13 @@ class MultiUBspline3D:
         _lib().einspline_gb300_wait_status(self.table)
         check()
 
+    def launch_shape(self, sorted: bool = False, vgh: bool = True):
+        """(tx, ty, pb, load mode) of a random-order or cell-sorted launch."""
+        v = [C.c_int() for _ in range(4)]
+        _lib().einspline_gb300_get_launch_shape(self.table, int(sorted), int(vgh), *[C.byref(x) for x in v])
+        check()
+        return tuple(x.value for x in v)
+
     def get_load_mode(self) -> int:
         r = _lib().einspline_gb300_get_load_mode(self.table)
         check()

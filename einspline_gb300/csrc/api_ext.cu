@@ -310,6 +310,15 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
   return 0;
 }
 
+int einspline_gb300_get_launch_shape(einspline_gb300_table *t, int sorted, int vgh, int *tx, int *ty, int *pb,
+                                     int *mode) {
+  clear();
+  if (!table3_ok(t) || !tx || !ty || !pb || !mode) return fail(EINSPLINE_GB300_EINVAL, "bad argument");
+  pick_tile(t, vgh != 0, 0, *tx, *ty, *pb, sorted != 0);
+  *mode = pick_mode(t, vgh != 0, sorted != 0);
+  return 0;
+}
+
 int einspline_gb300_get_load_mode(einspline_gb300_table *t) {
   clear();
   if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");

@@ -199,6 +199,10 @@ int einspline_gb300_autotune(einspline_gb300_table *t, int64_t npts, int vgh);
  * Sorted launches then use this choice; set_tile / set_load_mode still
  * override both; get_tile and get_load_mode report the random-order one. */
 int einspline_gb300_autotune_sorted(einspline_gb300_table *t, int64_t npts, int vgh);
+/* The tile and load mode a launch takes (random order or cell-sorted, vgh
+ * or value-only), after set_tile / set_load_mode, tuning and defaults. */
+int einspline_gb300_get_launch_shape(einspline_gb300_table *t, int sorted, int vgh, int *tx, int *ty, int *pb,
+                                     int *mode);
 
 /* --------------------------------------------------------------- serving */
 /* A request server over one table: QMC-walker-shaped requests (a set of

@@ -200,6 +200,8 @@ def test_sorted_tuning_changes_no_result(orc, storage):
     tile0, mode0 = G.get_tile(), G.get_load_mode()
     G.autotune(3000, sorted=True)
     assert G.get_tile() == tile0 and G.get_load_mode() == mode0
+    assert G.launch_shape() == tuple(tile0) + (mode0,)
+    assert all(x > 0 for x in G.launch_shape(sorted=True)[:3])
     for sort in (True, False):
         got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0, sort=sort)]
         for a, b in zip(got, base):
