@@ -209,11 +209,12 @@ def run_reference(args):
     with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
         list(ex.map(one, range(NSPL)))
     table = np.ascontiguousarray(T.coefs64.astype(np.float32))
-    del T
+    T.coefs64 = None
     rates = []
-    per_step = max(2.0, 20.0 / max(1, args.steps))
+    # a bounded sample per step: about 30 s of CPU work over the whole run
+    per_step = min(2.0, max(0.05, 30.0 / max(1, args.steps)))
     for _ in range(args.warmup):
-        cpu_eval_rate(table, NSPL, 0.5)
+        cpu_eval_rate(table, NSPL, min(0.5, per_step))
     for _ in range(args.steps):
         r, cores, sample = cpu_eval_rate(table, NSPL, per_step)
         rates.append(r)
@@ -223,8 +224,81 @@ def run_reference(args):
             "data": "synthetic", "config": workload_config(),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample + f"; median of {args.steps} steps"},
-            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_gpu": reference_gpu(args, table, T)}
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu(args, table, T):
+    """The reference's own CUDA vgh kernel (built for sm_103a from its sources,
+    oracle/ref_gpu.py) on this GPU: the same FP32 table and the same steps
+    as the library's FP32 loop, its outputs first checked against the oracle
+    on 64 points.  Kernel launches back to back on one stream (the
+    reference's entry adds a device synchronisation per call)."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+        torch.zeros(1, device="cuda")  # the context the module loads into
+        import ref_gpu
+        K = ref_gpu.RefVgh()
+    except Exception as e:  # module not built, no driver, kernel not found
+        return {"unavailable": str(e)}
+    coefs = torch.from_numpy(table).cuda()      # [67][67][67][1024]: the reference's _cuda layout
+    strides = ((GRID + 3) ** 2 * NSPL, (GRID + 3) * NSPL, NSPL)
+    dim, drinv = (GRID, GRID, GRID), (float(GRID),) * 3
+    batches = make_batches(args.warmup + max(1, args.steps), SEED_PTS)
+    maxp = max(p.shape[0] for p, _ in batches)
+    vals = torch.empty((maxp, NSPL), device="cuda")
+    grads = torch.empty((maxp, 3 * NSPL), device="cuda")
+    hess = torch.empty((maxp, 6 * NSPL), device="cuda")
+
+    def rows(t):
+        return torch.tensor([t.data_ptr() + i * t.shape[1] * 4 for i in range(maxp)], dtype=torch.int64,
+                            device="cuda")
+
+    vp, gp, hp = rows(vals), rows(grads), rows(hess)
+    pos = [torch.from_numpy(p.astype(np.float32)).cuda() for p, _ in batches]
+    stream = torch.cuda.current_stream()
+
+    def launch(k, num=None):
+        K.launch(pos[k].data_ptr(), num or pos[k].shape[0], drinv, coefs.data_ptr(), vp.data_ptr(), gp.data_ptr(),
+                 hp.data_ptr(), dim, strides, NSPL, stream.cuda_stream)
+
+    P0 = 64
+    launch(0, P0)
+    torch.cuda.synchronize()
+    x = batches[0][0][:P0].astype(np.float32).astype(np.float64)
+    rv, rg, rh = T.eval(x, vgh=True, sem=1, coefs=table)
+    rh6 = rh[..., [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+    check = {}
+    for name, got, ref in (("vals", vals[:P0].cpu().numpy(), rv),
+                           ("grads", grads[:P0].cpu().numpy().reshape(P0, NSPL, 3), rg),
+                           ("hess", hess[:P0].cpu().numpy().reshape(P0, NSPL, 6), rh6)):
+        scale = max(float(np.max(np.abs(ref))), 1e-30)
+        d = np.abs(got - ref)
+        check[name] = {"max_rel_err": float(np.max(d)) / scale, "entries_off_by_1e-4": float(np.mean(d > 1e-4 * scale))}
+    for k in range(args.warmup):
+        launch(k)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(args.warmup, len(batches)):
+        launch(k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    evals = sum(p.shape[0] for p, _ in batches[args.warmup:]) * NSPL
+    steps = len(batches) - args.warmup
+    return {"value": evals / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+            "kernel": "eval_multi_multi_UBspline_3d_s_vgh_kernel (src/multi_bspline_cuda_s_impl.h:342), "
+                      "FP32 table, 64-thread blocks, one point per block row",
+            "module": "oracle/_ref/multi_bspline_cuda_ref.cubin (src/multi_bspline_create_cuda.cu, nvcc sm_103a)",
+            "check_vs_oracle_64_points": check,
+            "note": "throughput of the reference kernel; its values and gradients are wrong in a few per cent of "
+                    "entries at 1024 splines: after its main loop each thread writes its gradients into the "
+                    "shared weight array abc (src/multi_bspline_cuda_s_impl.h:453-456) with no barrier, so "
+                    "the block's other warp can still be reading those weights"}
 
 
 def workload_config():

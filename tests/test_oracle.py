@@ -207,3 +207,16 @@ def test_live_reference_det_update(orc, N, k):
     ref = orc.ref_det_update(ainv, u - A[k], k).astype(np.float64)
     _, got = orc.sm_update(A, ainv, k, u)
     assert np.abs(got - ref).max() <= 5e-6 * np.abs(ref).max()
+
+
+def test_reference_gpu_basis_table(orc):
+    """The constant table the reference's GPU kernels read (Acuda, filled by
+    create_multi_UBspline_3d_s_cuda, src/multi_bspline_create_cuda.cu:428-441),
+    as the launcher builds it from the basis polynomials: power-basis rows
+    (t^3, t^2, t, 1) of b0..b3, their first and their second derivatives."""
+    import ref_gpu
+    s = 1.0 / 6.0
+    expect = [-s, 3 * s, -3 * s, s, 3 * s, -1.0, 0.0, 4 * s, -3 * s, 3 * s, 3 * s, s, s, 0.0, 0.0, 0.0,
+              0.0, -0.5, 1.0, -0.5, 0.0, 1.5, -2.0, 0.0, 0.0, -1.5, 1.0, 0.5, 0.0, 0.5, 0.0, 0.0,
+              0.0, 0.0, -1.0, 1.0, 0.0, 0.0, 3.0, -2.0, 0.0, 0.0, -3.0, 1.0, 0.0, 0.0, 1.0, 0.0]
+    assert np.array_equal(ref_gpu.basis_table(), np.asarray(expect, dtype=np.float32))
