@@ -290,15 +290,88 @@ def reference_gpu(args, table, T):
     ms = e0.elapsed_time(e1)
     evals = sum(p.shape[0] for p, _ in batches[args.warmup:]) * NSPL
     steps = len(batches) - args.warmup
+    del coefs, vals, grads, hess
+    torch.cuda.empty_cache()
+    other = {f"{kind}_{grid}cube_{nspl}": reference_gpu_config(K, kind, grid, nspl, npts, seed)
+             for kind, grid, nspl, npts, seed in (("d", 48, 512, 128 * 256, 203), ("c", 64, 256, 256 * 128, 304))}
     return {"value": evals / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
             "kernel": "eval_multi_multi_UBspline_3d_s_vgh_kernel (src/multi_bspline_cuda_s_impl.h:342), "
                       "FP32 table, 64-thread blocks, one point per block row",
             "module": "oracle/_ref/multi_bspline_cuda_ref.cubin (src/multi_bspline_create_cuda.cu, nvcc sm_103a)",
             "check_vs_oracle_64_points": check,
+            "other_configs": other,
             "note": "throughput of the reference kernel; its values and gradients are wrong in a few per cent of "
                     "entries at 1024 splines: after its main loop each thread writes its gradients into the "
                     "shared weight array abc (src/multi_bspline_cuda_s_impl.h:453-456) with no barrier, so "
                     "the block's other warp can still be reading those weights"}
+
+
+def reference_gpu_config(K, kind, grid, nspl, npts, seed):
+    """The reference's d or c vgh kernel on the FP64 (48^3 x 512) or complex
+    (64^3 x 256) batch of the library's other configurations: the same
+    points, one launch over all of them, on a random table of the same size
+    (throughput does not depend on the values), after a 16-point check
+    against the oracle on that table."""
+    import torch
+    import oracle as O
+    from einspline_gb300 import synth
+    real = torch.float64 if kind == "d" else torch.float32
+    ncol = 2 * nspl if kind == "c" else nspl
+    n3 = grid + 3
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    coefs = torch.rand((n3, n3, n3, ncol), dtype=real, device="cuda", generator=g) * 2 - 1
+    strides, dim, drinv = (n3 * n3 * ncol, n3 * ncol, ncol), (grid,) * 3, (float(grid),) * 3
+    pts = synth.points_uniform(seed, npts)
+    pos = torch.from_numpy(pts).to(real).cuda()
+    vals = torch.empty((npts, ncol), dtype=real, device="cuda")
+    grads = torch.empty((npts, 3 * ncol), dtype=real, device="cuda")
+    hess = torch.empty((npts, 6 * ncol), dtype=real, device="cuda")
+    es = vals.element_size()
+
+    def rows(t):
+        return torch.tensor([t.data_ptr() + i * t.shape[1] * es for i in range(npts)], dtype=torch.int64,
+                            device="cuda")
+
+    vp, gp, hp = rows(vals), rows(grads), rows(hess)
+    stream = torch.cuda.current_stream()
+
+    def launch(num):
+        K.launch(pos.data_ptr(), num, drinv, coefs.data_ptr(), vp.data_ptr(), gp.data_ptr(), hp.data_ptr(), dim,
+                 strides, nspl, stream.cuda_stream, kind=kind)
+
+    P0 = 16
+    launch(P0)
+    torch.cuda.synchronize()
+    cpx = kind == "c"
+    table = coefs.cpu().numpy()
+    T = O.Table(kind, [(0.0, 1.0, grid)] * 3, [(O.PERIODIC, O.PERIODIC)] * 3, nspl)
+    x = pts[:P0].astype(np.float32).astype(np.float64) if cpx else pts[:P0]
+    rv, rg, rh = T.eval(x, vgh=True, sem=1, coefs=table.reshape(table.shape[:3] + ((nspl, 2) if cpx else (nspl,))))
+    rh6 = rh[:, :, [0, 0, 0, 1, 1, 2], [0, 1, 2, 1, 2, 2]]
+    if cpx:  # GPU layout: [N][re, im][3 | 6]
+        rg, rh6 = np.swapaxes(rg, 2, 3), np.swapaxes(rh6, 2, 3)
+    check = {}
+    for name, got, ref in (("vals", vals[:P0], rv), ("grads", grads[:P0], rg), ("hess", hess[:P0], rh6)):
+        got = got.cpu().numpy().reshape(P0, -1)
+        ref = ref.reshape(P0, -1)
+        scale = max(float(np.max(np.abs(ref))), 1e-30)
+        d = np.abs(got - ref)
+        check[name] = {"max_rel_err": float(np.max(d)) / scale, "entries_off_by_1e-4": float(np.mean(d > 1e-4 * scale))}
+    launch(npts)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    reps = 5
+    e0.record(stream)
+    for _ in range(reps):
+        launch(npts)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    out = {"evals_per_s": npts * nspl / (ms / 1e3), "ms_per_launch": ms, "points": npts,
+           "kernel": f"eval_multi_multi_UBspline_3d_{kind}_vgh_kernel", "check_vs_oracle_16_points": check}
+    del coefs, vals, grads, hess, vp, gp, hp, pos
+    torch.cuda.empty_cache()
+    return out
 
 
 def workload_config():
