@@ -115,3 +115,37 @@ def test_host_entry_copy_and_direct_modes_agree(orc, mode):
     ref = [x.cpu().numpy() for x in G.eval(pos.cuda(), rule=0, layout=0)]
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_empty_batches_launch_nothing(orc):
+    """Zero points (or walkers) is a valid batch for every batched entry: no
+    kernel runs, nothing is written, no error is left.  A request server
+    refuses an empty request (there is nothing to wait for)."""
+    import torch
+    lib = L.load()
+    G, T, _ = build_pair(orc, "s", [(0.0, 1.0, 10)] * 3, [(P, P)] * 3, 6, seed=141)
+    C1 = G.to_cuda()
+    empty = torch.empty((0, 3), dtype=torch.float64, device="cuda")
+    n0 = api.launch_count()
+    for sort in (False, True):
+        v, g, h = G.eval(empty, sort=sort)
+        assert v.shape[0] == 0 and g.shape[0] == 0 and h.shape[0] == 0
+    v, g, h = G.eval_host(np.zeros((0, 3)))
+    assert v.shape[0] == 0
+    v, g, h = C1.eval_multi(empty.float())
+    assert v.shape[0] == 0
+    opts = L.EvalOpts(1, 1, 0, 0, 1, 0, 0, 0)
+    assert lib.einspline_gb300_eval_3d_sorted_noalloc(G.table, C.byref(opts), 0, C.c_void_p(1), C.c_void_p(1),
+                                                      C.c_void_p(1), C.c_void_p(1), None) == 0
+    dopts = L.DetOpts(6, 0, 6, 1, 0)
+    assert lib.einspline_gb300_det_ratio(G.table, C.byref(dopts), 0, *([None] * 7)) == 0
+    assert lib.einspline_gb300_det_update(C.byref(dopts), 0, None, None, None, None, None) == 0
+    torch.cuda.synchronize()
+    assert api.launch_count() == n0
+    assert lib.einspline_gb300_last_error() == 0
+    S = api.Server(G)
+    with pytest.raises(api.EinsplineError):
+        S.submit(np.zeros((0, 3)))
+    S.close()
+    C1.destroy()
