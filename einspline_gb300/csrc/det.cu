@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kDetThreads, kDetBlocksPerSM) k_det_ratio(cons
   extern __shared__ __align__(16) unsigned char smem[];
   const EvalArgs &a = d.e;
   const int64_t p0 = (int64_t)blockIdx.x * a.pb;
-  const int pn = eval_prologue<float>(a, smem, p0, threadIdx.x, kDetThreads);
+  const int pn = eval_prologue<float>(a, smem, p0, a.pb, threadIdx.x, kDetThreads);
   const float **sptr = reinterpret_cast<const float **>(smem + det_ptr_off(a.pb, RB));
   for (int q = threadIdx.x; q < pn; q += kDetThreads) sptr[q] = d.ainv[p0 + q];
   __syncthreads();

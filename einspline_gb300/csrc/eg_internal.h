@@ -198,7 +198,9 @@ struct EvalArgs {
   int layout;                 // 0 GPU layout, 1 CPU layout
   int is_complex;
   int ntiles;                 // column tiles per point group
-  int pb;                     // points per block
+  int pb;                     // points per block (shared-memory layout)
+  int pb_tail;                // > 0: point groups from g_tail on hold pb_tail points
+  int64_t g_tail;             //      (shorter blocks for the launch's last wave)
   int mode;                   // load mode: 0 direct loads, 1 L2 bulk prefetch first,
                               // 2/3 shared-memory pipeline of async copies,
                               // 4 shared-memory pipeline of tensor-map (TMA) copies

@@ -18,6 +18,10 @@
 #include <limits.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "eval_core.h"
 
 namespace eg {
@@ -194,8 +198,9 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
   int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
 
   const int tile = blockIdx.x % a.ntiles;
-  const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
-  const int pn = (int)min((int64_t)a.pb, a.npts - p0);
+  const int64_t grp = blockIdx.x / a.ntiles;
+  const int64_t p0 = group_first(a, grp);
+  const int pn = (int)min((int64_t)group_cap(a, grp), a.npts - p0);
   const int nthr = blockDim.x * blockDim.y;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   for (int q = tid; q < pn * 3; q += nthr) {
@@ -278,11 +283,12 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
   constexpr int NS = pipe_stages(ST, WIDE);
   extern __shared__ __align__(16) unsigned char smem[];
   const int tile = blockIdx.x % a.ntiles;
-  const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
+  const int64_t grp = blockIdx.x / a.ntiles;
+  const int64_t p0 = group_first(a, grp);
   // The wide variant always runs one warp per block, which makes every
   // shared-memory row offset below a compile-time constant.
   const int nthr = WIDE ? 32 : blockDim.x;
-  const int pn = eval_prologue<A>(a, smem, p0, threadIdx.x, nthr);
+  const int pn = eval_prologue<A>(a, smem, p0, group_cap(a, grp), threadIdx.x, nthr);
   __syncthreads();
   const A *sw = reinterpret_cast<const A *>(smem);
   const int *sidx = reinterpret_cast<const int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
@@ -372,10 +378,11 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
   constexpr int NS = TmaStages<ST>::value;
   extern __shared__ __align__(16) unsigned char smem[];
   const int tile = blockIdx.x % a.ntiles;
-  const int64_t p0 = (int64_t)(blockIdx.x / a.ntiles) * a.pb;
+  const int64_t grp = blockIdx.x / a.ntiles;
+  const int64_t p0 = group_first(a, grp);
   const int nthr = blockDim.x;
   if (threadIdx.x == 0) tma_prefetch_map(&a.tmap);
-  const int pn = eval_prologue<A>(a, smem, p0, threadIdx.x, nthr);
+  const int pn = eval_prologue<A>(a, smem, p0, group_cap(a, grp), threadIdx.x, nthr);
   const unsigned base_s = (unsigned)__cvta_generic_to_shared(smem);
   const unsigned pipe_s = (base_s + (unsigned)smem_total(a.pb, sizeof(A)) + 127u) & ~127u;
   const unsigned stage_bytes = 256u * (unsigned)nthr;
@@ -783,13 +790,59 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   return 0;
 }
 
+// Blocks of a kernel that one SM holds at once, looked up once per
+// (kernel, block size, shared memory) on the current device.
+static int resident_blocks(const void *func, int threads, size_t smem) {
+  struct Key {
+    const void *f;
+    int threads, dev;
+    size_t smem;
+    bool operator<(const Key &o) const {
+      return std::tie(f, threads, dev, smem) < std::tie(o.f, o.threads, o.dev, o.smem);
+    }
+  };
+  static std::mutex mu;
+  static std::map<Key, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return 0; }
+  const Key k{func, threads, dev, smem};
+  std::lock_guard<std::mutex> g(mu);
+  auto it = cache.find(k);
+  if (it != cache.end()) return it->second;
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, threads, smem) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return cache[k] = per_sm * sms;
+}
+
+// Point groups of a launch.  A launch of more than two waves gives the
+// points of its last wave of full groups to groups of pb/4 points: every
+// block computes its points the same way whatever its group holds, so the
+// results do not change, and the launch ends with short blocks instead of
+// SMs idling while the last full ones finish.
+static int64_t plan_groups(EvalArgs &a, const void *func, dim3 block, size_t smem) {
+  a.pb_tail = 0;
+  a.g_tail = 0;
+  const int64_t groups = (a.npts + a.pb - 1) / a.pb;
+  if (a.pb < 4) return groups;
+  const int64_t wave = (int64_t)resident_blocks(func, (int)(block.x * block.y), smem) / a.ntiles;
+  if (wave <= 0 || groups <= 2 * wave) return groups;
+  a.pb_tail = a.pb / 4;
+  a.g_tail = groups - wave;
+  const int64_t rest = a.npts - a.g_tail * a.pb;
+  return a.g_tail + (rest + a.pb_tail - 1) / a.pb_tail;
+}
+
 int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb) {
   if (a.npts <= 0) return 0;
   const void *func;
   dim3 block;
   size_t smem;
   if (int r = shape_launch(t, a, vgh, tx, ty, pb, &func, &block, &smem)) return r;
-  const int64_t blocks = ((a.npts + pb - 1) / pb) * a.ntiles;
+  const int64_t blocks = plan_groups(a, func, block, smem) * a.ntiles;
   if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
   cudaError_t e;
   switch (kernel_storage(t)) {
@@ -814,7 +867,7 @@ int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty,
 int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *grid,
                  dim3 *block, size_t *smem) {
   if (int r = shape_launch(t, a, vgh, tx, ty, pb, func, block, smem)) return r;
-  const int64_t blocks = ((a.npts + pb - 1) / pb) * a.ntiles;
+  const int64_t blocks = plan_groups(a, *func, *block, *smem) * a.ntiles;
   if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
   *grid = dim3((unsigned)(blocks > 0 ? blocks : 1));
   return 0;

@@ -427,13 +427,26 @@ __host__ __device__ __forceinline__ size_t smem_total(int pb, int accb) {
   return smem_w_bytes(pb, accb) + align_up((size_t)pb * 3 * 4, 8) + (size_t)pb * 8;
 }
 
-// Points' cells, weights and sources into shared memory (evaluation and determinant kernels).
+// Point group g of a launch (ntiles blocks each): its first point and the
+// number of points it may hold.  Groups hold pb points; with pb_tail > 0 the
+// groups from g_tail on hold pb_tail, so the blocks that run in the launch's
+// last wave are short and the SMs run out of work nearly together.
+__device__ __forceinline__ int64_t group_first(const EvalArgs &a, int64_t g) {
+  return (a.pb_tail == 0 || g < a.g_tail) ? g * a.pb : a.g_tail * a.pb + (g - a.g_tail) * a.pb_tail;
+}
+__device__ __forceinline__ int group_cap(const EvalArgs &a, int64_t g) {
+  return (a.pb_tail == 0 || g < a.g_tail) ? a.pb : a.pb_tail;
+}
+
+// Points' cells, weights and sources into shared memory (evaluation and
+// determinant kernels): at most cap points from p0.
 template <typename A>
-__device__ __forceinline__ int eval_prologue(const EvalArgs &a, unsigned char *smem, int64_t p0, int tid, int nthr) {
+__device__ __forceinline__ int eval_prologue(const EvalArgs &a, unsigned char *smem, int64_t p0, int cap, int tid,
+                                             int nthr) {
   A *sw = reinterpret_cast<A *>(smem);
   int *sidx = reinterpret_cast<int *>(smem + smem_w_bytes(a.pb, sizeof(A)));
   int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, sizeof(A)) + align_up((size_t)a.pb * 12, 8));
-  const int pn = (int)min((int64_t)a.pb, a.npts - p0);
+  const int pn = (int)min((int64_t)cap, a.npts - p0);
   for (int q = tid; q < pn * 3; q += nthr) {
     const int pp = q / 3, ax = q - 3 * pp;
     const int64_t src = a.perm ? (int64_t)a.perm[p0 + pp] : p0 + pp;

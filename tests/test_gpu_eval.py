@@ -123,6 +123,34 @@ def test_16bit_eval_matches_oracle_on_same_table(orc, storage):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("storage,mode", [(api.STORE_NATIVE, 0), (api.STORE_NATIVE, 2), (api.STORE_F16, 3),
+                                          (api.STORE_F16, 4)])
+def test_last_wave_groups_are_bit_identical(storage, mode):
+    """A batch of many waves gives its last wave's points to blocks of pb/4
+    points; results equal a launch of one point per block (no such split),
+    in every load mode, sorted and unsorted."""
+    import torch
+    G = api.MultiUBspline3D("s", PERIODIC_UNIT, [(P, P)] * 3, 45, storage=storage)
+    data = synth.grid_data_uniform(61, (14, 12, 13), 45, np.float32)
+    G.set_device(0, torch.from_numpy(data).cuda())
+    G.flush()
+    pt = torch_pos(synth.points_uniform(62, 120000, (0, 0, 0), (1, 1, 1)))
+    G.set_load_mode(0)
+    G.set_tile(32, 1, 1)
+    base = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
+    G.set_load_mode(mode)
+    for shape in [(32, 1, 8), (32, 1, 16), (64, 1, 5)]:
+        G.set_tile(*shape)
+        for srt in (False, True):
+            got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0, sort=srt)]
+            G.wait_status()
+            for a, b in zip(got, base):
+                assert np.array_equal(a, b), (shape, srt)
+    G.set_load_mode(-1)
+    G.set_tile(0, 0, 0)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("kind", "sz")
 def test_shapes_sorting_and_host_entry_are_bit_identical(orc, kind):
     """Results do not depend on the launch shape, on cell sorting, on batch
