@@ -53,37 +53,62 @@ __global__ void k_iota(int *p, int64_t n) {
 // right by `shift`, at most 16 per axis, 4096 keys), with each point's key
 // and the key counts held in shared memory.  Points within one coarse cell
 // come out in the order the atomics place them; each point still writes its
-// own output slot, so the results do not depend on that order.  (The radix
-// sort below takes three launches, ~40 us for 17k points.)
+// own output slot, so the results do not depend on that order.  The launch
+// is latency-bound (~28 us for 17k points, against ~40 us for the three
+// launches of the radix sort below); spreading it over a cluster of 8
+// blocks with distributed-shared-memory counts measured no faster.
 constexpr int kSmallSort = 32768;
-constexpr int kSmallSortThreads = 1024;
+constexpr int kSortThreads = 1024;
 constexpr int kCoarseKeys = 4096;
 constexpr size_t kSmallSortSmem = kCoarseKeys * 4 + kSmallSort * 2;
 
-__global__ void __launch_bounds__(kSmallSortThreads) k_sort_small(const EvalArgs a, int shift, int *perm) {
+// Morton interleave of three 4-bit coarse coordinates (12 bits).
+__device__ __forceinline__ unsigned spread4(unsigned v) {
+  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+
+// Coarse cell of one coordinate: FP32 is exact enough, since a point on the
+// wrong side of a coarse-cell edge only changes the visiting order.
+__device__ __forceinline__ unsigned coarse_cell(const EvalArgs &a, int ax, float x, int shift) {
+  const float u = a.rule == 0 ? (x - (float)a.start[ax]) * a.dinvf[ax] : x * a.dinvf[ax];
+  const int i = (int)floorf(u);
+  return (unsigned)(i < 0 ? 0 : (i > a.lim[ax] ? a.lim[ax] : i)) >> shift;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_small(const EvalArgs a, int shift, int *perm) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned *count = reinterpret_cast<unsigned *>(smem);
   unsigned short *key = reinterpret_cast<unsigned short *>(smem + kCoarseKeys * 4);
-  __shared__ unsigned warp_sum[kSmallSortThreads / 32];
+  __shared__ unsigned warp_sum[kSortThreads / 32];
   const int n = (int)a.npts, tid = threadIdx.x;
-  for (int k = tid; k < kCoarseKeys; k += kSmallSortThreads) count[k] = 0;
+  for (int k = tid; k < kCoarseKeys; k += kSortThreads) count[k] = 0;
   __syncthreads();
-  for (int p = tid; p < n; p += kSmallSortThreads) {
-    int c[3];
-    for (int ax = 0; ax < 3; ax++) {
-      const double xd = a.pos_f64 ? reinterpret_cast<const double *>(a.pos)[3 * (int64_t)p + ax]
-                                  : (double)reinterpret_cast<const float *>(a.pos)[3 * (int64_t)p + ax];
-      const double u = (a.rule == 0) ? (xd - a.start[ax]) * a.dinv[ax] : xd * a.dinv[ax];
-      const int i = (int)floor(u);
-      c[ax] = (i < 0 ? 0 : (i > a.lim[ax] ? a.lim[ax] : i)) >> shift;
+  // kBatch points a thread at a time, their coordinates loaded before any is used
+  constexpr int kBatch = 6;
+  for (int p0 = 0; p0 < n; p0 += kBatch * kSortThreads) {
+    float x[kBatch][3];
+#pragma unroll
+    for (int b = 0; b < kBatch; b++) {
+      const int p = p0 + b * kSortThreads + tid;
+#pragma unroll
+      for (int ax = 0; ax < 3; ax++)
+        x[b][ax] = p >= n ? 0.f
+                   : a.pos_f64 ? (float)reinterpret_cast<const double *>(a.pos)[3 * (int64_t)p + ax]
+                               : reinterpret_cast<const float *>(a.pos)[3 * (int64_t)p + ax];
     }
-    const unsigned k = (unsigned)((spread3(c[0]) << 2) | (spread3(c[1]) << 1) | spread3(c[2]));
-    key[p] = (unsigned short)k;
-    atomicAdd(&count[k], 1u);
+#pragma unroll
+    for (int b = 0; b < kBatch; b++) {
+      const int p = p0 + b * kSortThreads + tid;
+      if (p >= n) break;
+      const unsigned k = (spread4(coarse_cell(a, 0, x[b][0], shift)) << 2) |
+                         (spread4(coarse_cell(a, 1, x[b][1], shift)) << 1) | spread4(coarse_cell(a, 2, x[b][2], shift));
+      key[p] = (unsigned short)k;
+      atomicAdd(&count[k], 1u);
+    }
   }
   __syncthreads();
   // exclusive prefix sum of the counts: 4 keys a thread, then across warps
-  constexpr int per = kCoarseKeys / kSmallSortThreads;
+  constexpr int per = kCoarseKeys / kSortThreads;
   unsigned local[per], sum = 0;
 #pragma unroll
   for (int j = 0; j < per; j++) { local[j] = count[tid * per + j]; sum += local[j]; }
@@ -96,7 +121,8 @@ __global__ void __launch_bounds__(kSmallSortThreads) k_sort_small(const EvalArgs
   if ((tid & 31) == 31) warp_sum[tid >> 5] = incl;
   __syncthreads();
   if (tid < 32) {
-    unsigned w = warp_sum[tid], wi = w;
+    const unsigned w = warp_sum[tid];
+    unsigned wi = w;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const unsigned v = __shfl_up_sync(0xffffffffu, wi, d);
@@ -109,7 +135,7 @@ __global__ void __launch_bounds__(kSmallSortThreads) k_sort_small(const EvalArgs
 #pragma unroll
   for (int j = 0; j < per; j++) { count[tid * per + j] = run; run += local[j]; }
   __syncthreads();
-  for (int p = tid; p < n; p += kSmallSortThreads) perm[atomicAdd(&count[key[p]], 1u)] = p;
+  for (int p = tid; p < n; p += kSortThreads) perm[atomicAdd(&count[key[p]], 1u)] = p;
 }
 
 int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
@@ -136,7 +162,7 @@ int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
     // (an attribute of the kernel on the current device: set on every call)
     EG_CUDA(cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSortSmem));
     int *perm = (int *)t->sort_dev;
-    k_sort_small<<<1, kSmallSortThreads, kSmallSortSmem, s>>>(a, std::max(0, bits - 4), perm);
+    k_sort_small<<<1, kSortThreads, kSmallSortSmem, s>>>(a, std::max(0, bits - 4), perm);
     count_launch();
     EG_CUDA(cudaGetLastError());
     *perm_out = perm;
