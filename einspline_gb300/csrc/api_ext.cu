@@ -48,19 +48,23 @@ __global__ void k_iota(int *p, int64_t n) {
   if (i < n) p[i] = (int)i;
 }
 
-// Batches of up to kSmallSort points are ordered by one block in one launch:
-// a counting sort on the Morton key of coarse cells (the cell index shifted
-// right by `shift`, at most 16 per axis, 4096 keys), with each point's key
-// and the key counts held in shared memory.  Points within one coarse cell
-// come out in the order the atomics place them; each point still writes its
-// own output slot, so the results do not depend on that order.  The launch
-// is latency-bound (~28 us for 17k points, against ~40 us for the three
-// launches of the radix sort below); spreading it over a cluster of 8
-// blocks with distributed-shared-memory counts measured no faster.
+// Batches of up to kSmallSort points are ordered by a counting sort on the
+// Morton key of coarse cells (the cell index shifted right by `shift`, at
+// most 16 per axis, 4096 keys), in two launches of kSortBlocks blocks, block
+// b owning the b-th slice of the points.  k_sort_keys keys its slice and
+// writes the slice's key counts (row b of `hist`); k_sort_scatter gives key
+// k of slice b the offset (points with smaller keys) + (points with key k in
+// earlier slices) and places the slice's points with shared-memory atomics.
+// Points of one key within a slice come out in the order the atomics place
+// them; each point still writes its own output slot, so the results do not
+// depend on that order.  (One block doing all of it was latency-bound at
+// ~28 us for 17k points, an 8-block cluster no faster; the radix sort below
+// takes three launches, ~40 us.)
 constexpr int kSmallSort = 32768;
+constexpr int kSortBlocks = 16;
 constexpr int kSortThreads = 1024;
 constexpr int kCoarseKeys = 4096;
-constexpr size_t kSmallSortSmem = kCoarseKeys * 4 + kSmallSort * 2;
+constexpr int kKeysPerThread = kCoarseKeys / kSortThreads;
 
 // Morton interleave of three 4-bit coarse coordinates (12 bits).
 __device__ __forceinline__ unsigned spread4(unsigned v) {
@@ -75,43 +79,55 @@ __device__ __forceinline__ unsigned coarse_cell(const EvalArgs &a, int ax, float
   return (unsigned)(i < 0 ? 0 : (i > a.lim[ax] ? a.lim[ax] : i)) >> shift;
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_sort_small(const EvalArgs a, int shift, int *perm) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  unsigned *count = reinterpret_cast<unsigned *>(smem);
-  unsigned short *key = reinterpret_cast<unsigned short *>(smem + kCoarseKeys * 4);
-  __shared__ unsigned warp_sum[kSortThreads / 32];
-  const int n = (int)a.npts, tid = threadIdx.x;
+__device__ __forceinline__ void slice_of(int n, int b, int &lo, int &hi) {
+  const int chunk = (n + kSortBlocks - 1) / kSortBlocks;
+  lo = min(n, b * chunk);
+  hi = min(n, lo + chunk);
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_keys(const EvalArgs a, int shift, unsigned short *key,
+                                                            unsigned *hist) {
+  __shared__ unsigned count[kCoarseKeys];
+  const int tid = threadIdx.x;
+  int lo, hi;
+  slice_of((int)a.npts, blockIdx.x, lo, hi);
   for (int k = tid; k < kCoarseKeys; k += kSortThreads) count[k] = 0;
   __syncthreads();
-  // kBatch points a thread at a time, their coordinates loaded before any is used
-  constexpr int kBatch = 6;
-  for (int p0 = 0; p0 < n; p0 += kBatch * kSortThreads) {
-    float x[kBatch][3];
+  for (int p = lo + tid; p < hi; p += kSortThreads) {
+    float x[3];
 #pragma unroll
-    for (int b = 0; b < kBatch; b++) {
-      const int p = p0 + b * kSortThreads + tid;
-#pragma unroll
-      for (int ax = 0; ax < 3; ax++)
-        x[b][ax] = p >= n ? 0.f
-                   : a.pos_f64 ? (float)reinterpret_cast<const double *>(a.pos)[3 * (int64_t)p + ax]
-                               : reinterpret_cast<const float *>(a.pos)[3 * (int64_t)p + ax];
-    }
-#pragma unroll
-    for (int b = 0; b < kBatch; b++) {
-      const int p = p0 + b * kSortThreads + tid;
-      if (p >= n) break;
-      const unsigned k = (spread4(coarse_cell(a, 0, x[b][0], shift)) << 2) |
-                         (spread4(coarse_cell(a, 1, x[b][1], shift)) << 1) | spread4(coarse_cell(a, 2, x[b][2], shift));
-      key[p] = (unsigned short)k;
-      atomicAdd(&count[k], 1u);
-    }
+    for (int ax = 0; ax < 3; ax++)
+      x[ax] = a.pos_f64 ? (float)reinterpret_cast<const double *>(a.pos)[3 * (int64_t)p + ax]
+                        : reinterpret_cast<const float *>(a.pos)[3 * (int64_t)p + ax];
+    const unsigned k = (spread4(coarse_cell(a, 0, x[0], shift)) << 2) |
+                       (spread4(coarse_cell(a, 1, x[1], shift)) << 1) | spread4(coarse_cell(a, 2, x[2], shift));
+    key[p] = (unsigned short)k;
+    atomicAdd(&count[k], 1u);
   }
   __syncthreads();
-  // exclusive prefix sum of the counts: 4 keys a thread, then across warps
-  constexpr int per = kCoarseKeys / kSortThreads;
-  unsigned local[per], sum = 0;
+  uint4 c;
+  c.x = count[kKeysPerThread * tid]; c.y = count[kKeysPerThread * tid + 1];
+  c.z = count[kKeysPerThread * tid + 2]; c.w = count[kKeysPerThread * tid + 3];
+  reinterpret_cast<uint4 *>(hist + (size_t)blockIdx.x * kCoarseKeys)[tid] = c;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(int n, const unsigned short *key,
+                                                               const unsigned *hist, int *perm) {
+  static_assert(kKeysPerThread == 4, "one uint4 of counts a thread");
+  __shared__ unsigned count[kCoarseKeys];
+  __shared__ unsigned warp_sum[kSortThreads / 32];
+  const int tid = threadIdx.x, b = blockIdx.x;
+  // this thread's 4 keys: their totals and the counts of earlier slices
+  unsigned tot[4] = {0, 0, 0, 0}, before[4] = {0, 0, 0, 0};
 #pragma unroll
-  for (int j = 0; j < per; j++) { local[j] = count[tid * per + j]; sum += local[j]; }
+  for (int r = 0; r < kSortBlocks; r++) {
+    const uint4 c = reinterpret_cast<const uint4 *>(hist + (size_t)r * kCoarseKeys)[tid];
+    tot[0] += c.x; tot[1] += c.y; tot[2] += c.z; tot[3] += c.w;
+    if (r < b) { before[0] += c.x; before[1] += c.y; before[2] += c.z; before[3] += c.w; }
+  }
+  // exclusive prefix sum of the totals over the keys: within the thread,
+  // then across lanes and warps
+  const unsigned sum = tot[0] + tot[1] + tot[2] + tot[3];
   unsigned incl = sum;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
@@ -133,9 +149,14 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_small(const EvalArgs a, i
   __syncthreads();
   unsigned run = warp_sum[tid >> 5] + incl - sum;
 #pragma unroll
-  for (int j = 0; j < per; j++) { count[tid * per + j] = run; run += local[j]; }
+  for (int j = 0; j < 4; j++) {
+    count[4 * tid + j] = run + before[j];
+    run += tot[j];
+  }
   __syncthreads();
-  for (int p = tid; p < n; p += kSortThreads) perm[atomicAdd(&count[key[p]], 1u)] = p;
+  int lo, hi;
+  slice_of(n, b, lo, hi);
+  for (int p = lo + tid; p < hi; p += kSortThreads) perm[atomicAdd(&count[key[p]], 1u)] = p;
 }
 
 int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
@@ -148,7 +169,9 @@ int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
     bits = std::max(bits, b);
   }
   if (n <= kSmallSort) {
-    const size_t need = align_up_sz(n * 4, 256);
+    // perm, the keys, then the slices' key counts
+    const size_t key_off = align_up_sz(n * 4, 256), hist_off = key_off + align_up_sz(n * 2, 256);
+    const size_t need = hist_off + (size_t)kSortBlocks * kCoarseKeys * 4;
     if (t->sort_bytes < need) {
       cudaFree(t->sort_dev);
       t->sort_dev = nullptr;
@@ -159,11 +182,13 @@ int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
       }
       t->sort_bytes = need;
     }
-    // (an attribute of the kernel on the current device: set on every call)
-    EG_CUDA(cudaFuncSetAttribute(k_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSortSmem));
-    int *perm = (int *)t->sort_dev;
-    k_sort_small<<<1, kSortThreads, kSmallSortSmem, s>>>(a, std::max(0, bits - 4), perm);
-    count_launch();
+    char *base = (char *)t->sort_dev;
+    int *perm = (int *)base;
+    unsigned short *key = (unsigned short *)(base + key_off);
+    unsigned *hist = (unsigned *)(base + hist_off);
+    k_sort_keys<<<kSortBlocks, kSortThreads, 0, s>>>(a, std::max(0, bits - 4), key, hist);
+    k_sort_scatter<<<kSortBlocks, kSortThreads, 0, s>>>((int)n, key, hist, perm);
+    count_launch(2);
     EG_CUDA(cudaGetLastError());
     *perm_out = perm;
     return 0;

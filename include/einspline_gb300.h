@@ -117,7 +117,9 @@ typedef struct {
                      grads [N][re,im][3]; 1: CPU layout -- hess [N][3][3],
                      complex grads [N][3][re,im]                              */
   int sort;       /* 1: visit points in cell (Morton) order for L2 reuse; the
-                     results are bit-identical to sort = 0                    */
+                     results are bit-identical to sort = 0.  The ordering
+                     uses the table's sort scratch: sorted calls on one
+                     table on different streams must not overlap          */
   int64_t vstride, gstride, hstride; /* per-point output strides in output
                      reals (float for s/c, double for d/z); 0 = packed       */
 } einspline_gb300_eval_opts;
