@@ -220,3 +220,27 @@ def test_reference_gpu_basis_table(orc):
               0.0, -0.5, 1.0, -0.5, 0.0, 1.5, -2.0, 0.0, 0.0, -1.5, 1.0, 0.5, 0.0, 0.5, 0.0, 0.0,
               0.0, 0.0, -1.0, 1.0, 0.0, 0.0, 3.0, -2.0, 0.0, 0.0, -3.0, 1.0, 0.0, 0.0, 1.0, 0.0]
     assert np.array_equal(ref_gpu.basis_table(), np.asarray(expect, dtype=np.float32))
+
+
+def test_planewave_interpolation_converges(orc):
+    """The analytic known-answer pattern of the reference's single-spline
+    tests (src/test_bspline_d.c:40-188: a periodic plane-wave sum,
+    interpolated and compared with its analytic value, gradient and Hessian;
+    the reference prints the errors without a threshold).  Here the errors
+    must fall at the cubic spline's rates as the grid is refined."""
+    from einspline_gb300 import synth
+    from helpers import CONVERGENCE_RATIOS, planewave_analytic, rms_rel
+    S = 8
+    pos = synth.points_uniform(91, 2000)
+    err = {}
+    for M in (24, 48):
+        data, k, amp = synth.grid_data_planewaves(90, (M, M, M), S, waves=8, kmax=2, noise=0.0)
+        T = orc.Table("d", [(0.0, 1.0, M)] * 3, [(0, 0)] * 3, S)
+        for i in range(S):
+            T.set_spline(i, data[i])
+        v, g, h = T.eval(pos, vgh=True, sem=0)
+        va, ga, ha = planewave_analytic(k, amp, pos)
+        err[M] = (rms_rel(v, va), rms_rel(g, ga), rms_rel(h.reshape(ha.shape), ha))
+    for q, (lo, hi) in enumerate(CONVERGENCE_RATIOS):
+        assert lo <= err[24][q] / err[48][q] <= hi, (q, err)
+    assert err[48][0] < 3e-5 and err[48][1] < 3e-4 and err[48][2] < 5e-3, err
