@@ -287,3 +287,46 @@ def test_planewave_interpolation_converges_on_gpu(kind, storage):
     for q, (lo, hi) in enumerate(CONVERGENCE_RATIOS):
         assert lo <= err[24][q] / err[48][q] <= hi, (q, err)
     assert err[48][0] < 3e-5 and err[48][1] < 3e-4 and err[48][2] < 5e-3, err
+
+
+# The reference's own tolerance ladder (src/test_multi.c: absolute
+# differences, value / gradient / Hessian; 1e-6 / 1e-4 / 1e-3 in single
+# precision, :345, :364, :418; 1e-12 / 1e-10 / 1e-10 in double, :768, :793, :822).
+LADDER = {"s": (1e-6, 1e-4, 1e-3), "c": (1e-6, 1e-4, 1e-3), "d": (1e-12, 1e-10, 1e-10), "z": (1e-12, 1e-10, 1e-10)}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["s_periodic", "s_mixed", "d_periodic", "d_mixed", "c_periodic", "c_mixed",
+                                  "z_periodic", "z_mixed"])
+def test_gpu_matches_reference_outputs_within_its_ladder(name):
+    """The library, fed through the reference's create/set entries, against
+    the outputs the compiled reference itself produced for the same data and
+    points (tests/golden, made by tests/golden/make_golden.py), within the
+    absolute tolerances the reference's own multi-spline test uses: the
+    CPU-shaped single-point entry and the batched entry (CPU layout)."""
+    import os
+    import torch
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    kind = str(z["kind"])
+    grids = [tuple(g[:2]) + (int(g[2]),) for g in z["grids"]]
+    bcs = [tuple([int(b[0]), int(b[1])] + list(b[2:])) for b in z["bcs"]]
+    N = int(z["num_splines"])
+    G = api.MultiUBspline3D(kind, grids, bcs, N)
+    for i in range(N):
+        G.set(i, z["data"][i])
+    G.flush()
+    tv, tg, th = LADDER[kind]
+    pos = z["pos"]
+    ref = (z["vals"], z["grads"], z["hess"])
+    batched = [x.cpu().numpy() for x in G.eval(torch_pos(pos), rule=0, layout=1)]
+    for got, want, tol, what in zip(batched, ref, (tv, tg, th), ("value", "gradient", "hessian")):
+        d = np.abs(got.reshape(want.shape).astype(np.float64) - want).max()
+        assert d <= tol, (name, "batched", what, d)
+    for p in range(0, pos.shape[0], 7):
+        v, g, h = G.eval_point(*pos[p])
+        for got, want, tol, what in zip((v, g, h), (ref[0][p], ref[1][p], ref[2][p]), (tv, tg, th),
+                                        ("value", "gradient", "hessian")):
+            d = np.abs(np.asarray(got).reshape(want.shape).astype(np.float64) - want).max()
+            assert d <= tol, (name, "point", p, what, d)
+    v0 = G.eval(torch_pos(pos), vgh=False, rule=0, layout=1)[0].cpu().numpy()
+    assert np.abs(v0.reshape(z["value"].shape).astype(np.float64) - z["value"]).max() <= tv
