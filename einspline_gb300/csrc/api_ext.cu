@@ -50,18 +50,20 @@ __global__ void k_iota(int *p, int64_t n) {
 
 // Batches of up to kSmallSort points are ordered by a counting sort on the
 // Morton key of coarse cells (the cell index shifted right by `shift`, at
-// most 16 per axis, 4096 keys), in two launches of kSortBlocks blocks, block
-// b owning the b-th slice of the points.  k_sort_keys keys its slice and
+// most 16 per axis, 4096 keys), in two launches of S blocks (16, or one per
+// kSortSlice points beyond that), block b owning the b-th slice of the
+// points.  k_sort_keys keys its slice and
 // writes the slice's key counts (row b of `hist`); k_sort_scatter gives key
 // k of slice b the offset (points with smaller keys) + (points with key k in
 // earlier slices) and places the slice's points with shared-memory atomics.
 // Points of one key within a slice come out in the order the atomics place
 // them; each point still writes its own output slot, so the results do not
 // depend on that order.  (One block doing all of it was latency-bound at
-// ~28 us for 17k points, an 8-block cluster no faster; the radix sort below
-// takes three launches, ~40 us.)
-constexpr int kSmallSort = 32768;
-constexpr int kSortBlocks = 16;
+// ~28 us for 17k points, an 8-block cluster no faster; the radix sort below,
+// for larger batches, takes three launches, ~40 us at 17k points.)
+constexpr int kSmallSort = 131072;
+constexpr int kSortSlice = 2048;  // most points a slice holds
+constexpr int kSortMinBlocks = 16;
 constexpr int kSortThreads = 1024;
 constexpr int kCoarseKeys = 4096;
 constexpr int kKeysPerThread = kCoarseKeys / kSortThreads;
@@ -80,7 +82,7 @@ __device__ __forceinline__ unsigned coarse_cell(const EvalArgs &a, int ax, float
 }
 
 __device__ __forceinline__ void slice_of(int n, int b, int &lo, int &hi) {
-  const int chunk = (n + kSortBlocks - 1) / kSortBlocks;
+  const int chunk = (n + (int)gridDim.x - 1) / (int)gridDim.x;
   lo = min(n, b * chunk);
   hi = min(n, lo + chunk);
 }
@@ -119,8 +121,8 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(int n, const unsi
   const int tid = threadIdx.x, b = blockIdx.x;
   // this thread's 4 keys: their totals and the counts of earlier slices
   unsigned tot[4] = {0, 0, 0, 0}, before[4] = {0, 0, 0, 0};
-#pragma unroll
-  for (int r = 0; r < kSortBlocks; r++) {
+#pragma unroll 4
+  for (int r = 0; r < (int)gridDim.x; r++) {
     const uint4 c = reinterpret_cast<const uint4 *>(hist + (size_t)r * kCoarseKeys)[tid];
     tot[0] += c.x; tot[1] += c.y; tot[2] += c.z; tot[3] += c.w;
     if (r < b) { before[0] += c.x; before[1] += c.y; before[2] += c.z; before[3] += c.w; }
@@ -171,7 +173,8 @@ int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
   if (n <= kSmallSort) {
     // perm, the keys, then the slices' key counts
     const size_t key_off = align_up_sz(n * 4, 256), hist_off = key_off + align_up_sz(n * 2, 256);
-    const size_t need = hist_off + (size_t)kSortBlocks * kCoarseKeys * 4;
+    const int S = (int)std::max<int64_t>(kSortMinBlocks, (n + kSortSlice - 1) / kSortSlice);
+    const size_t need = hist_off + (size_t)S * kCoarseKeys * 4;
     if (t->sort_bytes < need) {
       cudaFree(t->sort_dev);
       t->sort_dev = nullptr;
@@ -186,8 +189,8 @@ int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
     int *perm = (int *)base;
     unsigned short *key = (unsigned short *)(base + key_off);
     unsigned *hist = (unsigned *)(base + hist_off);
-    k_sort_keys<<<kSortBlocks, kSortThreads, 0, s>>>(a, std::max(0, bits - 4), key, hist);
-    k_sort_scatter<<<kSortBlocks, kSortThreads, 0, s>>>((int)n, key, hist, perm);
+    k_sort_keys<<<S, kSortThreads, 0, s>>>(a, std::max(0, bits - 4), key, hist);
+    k_sort_scatter<<<S, kSortThreads, 0, s>>>((int)n, key, hist, perm);
     count_launch(2);
     EG_CUDA(cudaGetLastError());
     *perm_out = perm;

@@ -152,15 +152,15 @@ def test_last_wave_groups_are_bit_identical(storage, mode):
 
 @pytest.mark.gpu
 def test_sorted_batches_of_changing_size_share_the_sort_scratch():
-    """Sorted calls on one table alternate between the small-batch counting
-    sort (up to 32,768 points, key counts kept zero between calls) and the
-    radix sort of larger batches over the same scratch; every call equals
-    the unsorted evaluation bit for bit."""
+    """Sorted calls on one table alternate between the counting sort (up
+    to 131,072 points, 16 to 64 slices) and the radix sort of larger batches
+    over the same scratch; every call equals the unsorted evaluation bit for
+    bit."""
     import torch
     G = api.MultiUBspline3D("s", PERIODIC_UNIT, [(P, P)] * 3, 45, storage=api.STORE_F16)
     G.set_device(0, torch.from_numpy(synth.grid_data_uniform(71, (14, 12, 13), 45, np.float32)).cuda())
     G.flush()
-    for i, n in enumerate([5000, 40000, 3000, 3001, 32768, 32769, 2, 100, 17000]):
+    for i, n in enumerate([5000, 140000, 3000, 3001, 32768, 32769, 2, 100, 131072, 131073, 70000, 17000]):
         pt = torch_pos(synth.points_uniform(72 + i, n, (0, 0, 0), (1, 1, 1)))
         base = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0)]
         got = [x.cpu().numpy() for x in G.eval(pt, rule=0, layout=0, sort=True)]
