@@ -407,16 +407,17 @@ def run_gpu(args):
         if args.autotune:
             t.autotune(int(np.mean(npts)), True)
             t.autotune(int(np.mean(npts)), True, sorted=True)
+            t.autotune(int(np.mean(npts)), False)
 
     for t in tabs.values():
         tune(t)
     tiles = {k: {"tile": list(t.get_tile()), "load_mode": t.get_load_mode(),
                  "sorted_tile_and_mode": list(t.launch_shape(sorted=True))} for k, t in tabs.items()}
 
-    def timed(t, sort=False):
+    def timed(t, sort=False, vgh=True):
         for k in range(args.warmup):
             P = npts[k]
-            t.eval(pos_d[k], vgh=True, rule=0, layout=0, sort=sort, out=(out[0][:P], out[1][:P], out[2][:P]))
+            t.eval(pos_d[k], vgh=vgh, rule=0, layout=0, sort=sort, out=(out[0][:P], out[1][:P], out[2][:P]))
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -426,7 +427,7 @@ def run_gpu(args):
         evals = 0
         for k in range(args.warmup, nb):
             P = npts[k]
-            t.eval(pos_d[k], vgh=True, rule=0, layout=0, sort=sort, out=(out[0][:P], out[1][:P], out[2][:P]))
+            t.eval(pos_d[k], vgh=vgh, rule=0, layout=0, sort=sort, out=(out[0][:P], out[1][:P], out[2][:P]))
             evals += P * NSPL
         e1.record(stream)
         torch.cuda.synchronize()
@@ -443,6 +444,9 @@ def run_gpu(args):
         evi, msi, _ = timed(tabs["i16"])
         ev16s, ms16s, l16s = timed(tabs["f16"], sort=True)
         ev32s, ms32s, _ = timed(tabs["f32"], sort=True)
+        # value only (the reference's eval_multi_multi_*_cuda without derivatives)
+        ev16v, ms16v, _ = timed(tabs["f16"], vgh=False)
+        ev32v, ms32v, _ = timed(tabs["f32"], vgh=False)
         # repeat the headline loop once more so the sampler sees sustained load
         ev16b, ms16b, _ = timed(tabs["f16"])
     ms16 = min(ms16, ms16b) if args.steps > 0 else ms16
@@ -560,6 +564,10 @@ def run_gpu(args):
         "fp16_vs_fp32": rate16 / rate32,
         "tiles": tiles,
         "i16_table": {"value": evi / (msi / 1e3), "ms_per_step": msi / args.steps},
+        "value_only": {"f16_value": ev16v / (ms16v / 1e3), "f32_value": ev32v / (ms32v / 1e3),
+                       "bytes_per_eval": {"f16": 64 * 2 + 4, "f32": 64 * 4 + 4},
+                       "f16_achieved_GBps": ev16v / (ms16v / 1e3) / world * (64 * 2 + 4) / 1e9,
+                       "shapes": {k: list(tabs[k].launch_shape(vgh=False)) for k in ("f16", "f32")}},
         "cell_sorted": {"f16_value": ev16s / (ms16s / 1e3), "f32_value": ev32s / (ms32s / 1e3),
                         "launches_per_step": l16s / max(1, args.steps),
                         "note": "points visited in Morton order of their cells (sort kernels inside the timed region)"},
