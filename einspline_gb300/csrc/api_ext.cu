@@ -52,10 +52,10 @@ __global__ void k_iota(int *p, int64_t n) {
 // Morton key of coarse cells (the cell index shifted right by `shift`, at
 // most 16 per axis, 4096 keys), in two launches of S blocks (16, or one per
 // kSortSlice points beyond that), block b owning the b-th slice of the
-// points.  k_sort_keys keys its slice and
-// writes the slice's key counts (row b of `hist`); k_sort_scatter gives key
-// k of slice b the offset (points with smaller keys) + (points with key k in
-// earlier slices) and places the slice's points with shared-memory atomics.
+// points.  k_sort_keys keys its slice and writes the slice's key counts
+// (row b of `hist`); k_sort_scatter gives key k of slice b the offset
+// (points with smaller keys) + (points with key k in earlier slices) and
+// places the slice's points with shared-memory atomics.
 // Points of one key within a slice come out in the order the atomics place
 // them; each point still writes its own output slot, so the results do not
 // depend on that order.  (One block doing all of it was latency-bound at
