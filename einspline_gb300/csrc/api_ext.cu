@@ -61,7 +61,6 @@ __global__ void k_iota(int *p, int64_t n) {
 // depend on that order.  (One block doing all of it was latency-bound at
 // ~28 us for 17k points, an 8-block cluster no faster; the radix sort below,
 // for larger batches, takes three launches, ~40 us at 17k points.)
-constexpr int kSmallSort = 131072;
 constexpr int kSortSlice = 2048;  // most points a slice holds
 constexpr int kSortMinBlocks = 16;
 constexpr int kSortThreads = 1024;
@@ -161,6 +160,39 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(int n, const unsi
   for (int p = lo + tid; p < hi; p += kSortThreads) perm[atomicAdd(&count[key[p]], 1u)] = p;
 }
 
+static int coarse_shift(const EvalArgs &a) {
+  int bits = 0;
+  for (int ax = 0; ax < 3; ax++) {
+    int b = 1;
+    while ((1 << b) <= a.lim[ax]) b++;
+    bits = std::max(bits, b);
+  }
+  return std::max(0, bits - 4);
+}
+
+static int sort_slices(int64_t n) { return (int)std::max<int64_t>(kSortMinBlocks, (n + kSortSlice - 1) / kSortSlice); }
+
+// Scratch of the counting sort of n <= kSmallSort points: perm, the keys,
+// then the slices' key counts.
+size_t small_sort_bytes(int64_t n) {
+  return align_up_sz(n * 4, 256) + align_up_sz(n * 2, 256) + (size_t)sort_slices(n) * kCoarseKeys * 4;
+}
+
+int small_sort_into(const EvalArgs &a, void *scratch, int **perm_out, cudaStream_t s) {
+  const int64_t n = a.npts;
+  const int S = sort_slices(n);
+  char *base = (char *)scratch;
+  int *perm = (int *)base;
+  unsigned short *key = (unsigned short *)(base + align_up_sz(n * 4, 256));
+  unsigned *hist = (unsigned *)(base + align_up_sz(n * 4, 256) + align_up_sz(n * 2, 256));
+  k_sort_keys<<<S, kSortThreads, 0, s>>>(a, coarse_shift(a), key, hist);
+  k_sort_scatter<<<S, kSortThreads, 0, s>>>((int)n, key, hist, perm);
+  count_launch(2);
+  EG_CUDA(cudaGetLastError());
+  *perm_out = perm;
+  return 0;
+}
+
 int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
   const int64_t n = a.npts;
   if (n > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "sorted evaluation takes at most %d points", INT_MAX);
@@ -171,10 +203,7 @@ int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
     bits = std::max(bits, b);
   }
   if (n <= kSmallSort) {
-    // perm, the keys, then the slices' key counts
-    const size_t key_off = align_up_sz(n * 4, 256), hist_off = key_off + align_up_sz(n * 2, 256);
-    const int S = (int)std::max<int64_t>(kSortMinBlocks, (n + kSortSlice - 1) / kSortSlice);
-    const size_t need = hist_off + (size_t)S * kCoarseKeys * 4;
+    const size_t need = small_sort_bytes(n);
     if (t->sort_bytes < need) {
       cudaFree(t->sort_dev);
       t->sort_dev = nullptr;
@@ -185,16 +214,7 @@ int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
       }
       t->sort_bytes = need;
     }
-    char *base = (char *)t->sort_dev;
-    int *perm = (int *)base;
-    unsigned short *key = (unsigned short *)(base + key_off);
-    unsigned *hist = (unsigned *)(base + hist_off);
-    k_sort_keys<<<S, kSortThreads, 0, s>>>(a, std::max(0, bits - 4), key, hist);
-    k_sort_scatter<<<S, kSortThreads, 0, s>>>((int)n, key, hist, perm);
-    count_launch(2);
-    EG_CUDA(cudaGetLastError());
-    *perm_out = perm;
-    return 0;
+    return small_sort_into(a, t->sort_dev, perm_out, s);
   }
   const int end_bit = std::min(63, 3 * bits);
   size_t temp = 0;

@@ -240,6 +240,12 @@ int elems_per_thread(const Table *t);
 
 // sorting
 int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s);
+// The counting sort of batches of up to kSmallSort points into caller-given
+// scratch of small_sort_bytes(npts) bytes (16-byte aligned; nothing in it
+// has to start at zero).
+constexpr int64_t kSmallSort = 131072;
+size_t small_sort_bytes(int64_t n);
+int small_sort_into(const EvalArgs &a, void *scratch, int **perm_out, cudaStream_t s);
 // Morton key of each point's cell and its index (defined in api_ext.cu).
 __global__ void k_cell_keys(const EvalArgs a, uint64_t *keys, int *idx);
 

@@ -1,8 +1,9 @@
 // Cell-sorted batched evaluation that allocates no memory.
 //
 // einspline_gb300_eval_3d with opts.sort = 1 sorts the points by cell in a
-// scratch area (keys, indices and the radix sort's work space) that it
-// allocates with cudaMalloc and keeps on the table.  Some callers cannot let
+// scratch area (keys, key counts and the visiting order, or the radix sort's
+// work space for large batches) that it allocates with cudaMalloc and keeps
+// on the table.  Some callers cannot let
 // a library allocate device memory while they run: QMC drivers that hand the
 // whole device to their own pool allocator and account for every byte, code
 // that runs while another component holds the device's allocation lock, or
@@ -95,6 +96,16 @@ extern "C" int einspline_gb300_eval_3d_sorted_noalloc(einspline_gb300_table *t, 
   a.pos = pos_d;
   a.vals = vals_d; a.grads = grads_d; a.hess = hess_d;
 
+  int tx, ty, pb;
+  pick_tile(t, o->vgh != 0, npts, tx, ty, pb, true);
+  // Batches of up to kSmallSort points: the two-launch counting sort, whose
+  // scratch (under 2 MB) is written before it is read.
+  if (npts <= kSmallSort && small_sort_bytes(npts) <= kScratchBytes) {
+    int *perm = nullptr;
+    if (int r = small_sort_into(a, scratch, &perm, s)) return r;
+    a.perm = perm;
+    return launch_eval(t, a, o->vgh != 0, s, tx, ty, pb);
+  }
   char *p = (char *)scratch;
   uint64_t *k_in = (uint64_t *)p;
   uint64_t *k_out = (uint64_t *)(p + kKeyBytes);
@@ -120,7 +131,5 @@ extern "C" int einspline_gb300_eval_3d_sorted_noalloc(einspline_gb300_table *t, 
   EG_CUDA(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, k_in, k_out, v_in, v_out, (int)npts, 0, end_bit, s));
   count_launch();
   a.perm = v_out;
-  int tx, ty, pb;
-  pick_tile(t, o->vgh != 0, npts, tx, ty, pb, true);
   return launch_eval(t, a, o->vgh != 0, s, tx, ty, pb);
 }

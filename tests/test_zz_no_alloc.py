@@ -37,8 +37,10 @@ def test_noalloc_sorted_matches_allocating_entry(kind):
     G.flush()
     dt = torch.float32 if kind == "s" else torch.float64
     opts = L.EvalOpts(1, 1, 0, 0, 1, 0, 0, 0)
-    for call, seed in enumerate((11, 12)):  # two calls in a row share the scratch
-        pos = torch.from_numpy(synth.points_uniform(seed, 5000 + 37 * call)).cuda()
+    # two calls in a row share the scratch (counting sort), then a batch large
+    # enough for the radix sort in the same scratch
+    for call, (seed, n) in enumerate(((11, 5000), (12, 5037), (13, 140000))):
+        pos = torch.from_numpy(synth.points_uniform(seed, n)).cuda()
         P = pos.shape[0]
         ref = G.eval(pos, vgh=True, rule=0, layout=0, sort=True)
         out = (torch.full((P, N), -1.0, dtype=dt, device="cuda"), torch.full((P, N, 3), -1.0, dtype=dt, device="cuda"),
