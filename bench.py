@@ -526,17 +526,19 @@ def run_gpu(args):
         sizes = synth.walker_sizes(4252, n)
         arr = synth.poisson_arrivals(4253, n, 2.0 * cap)
         pts = synth.points_uniform(4254, int(sizes.sum()))
-        for name in ("f16", "f32"):
-            srv = api.Server(tabs[name], max_inflight=3, max_batch_points=16384)
+        for name, srt in (("f16", False), ("f32", False), ("f16", True), ("f32", True)):
+            srv = api.Server(tabs[name], max_inflight=3, max_batch_points=16384, sort=srt)
             w = min(n, 200)
             srv.replay(np.arange(w) * 1e-5, sizes[:w], pts[: int(sizes[:w].sum())])
             _, wall = srv.replay(arr, sizes, pts)
             srv.close()
-            sat[name] = float(sizes.sum() * NSPL / wall)
+            sat[name + ("_sorted" if srt else "")] = float(sizes.sum() * NSPL / wall)
         serving_stats["saturated"] = {
             "offered_load": 2.0, "requests": n, "f16_evals_per_s": sat["f16"] * world,
             "f32_evals_per_s": sat["f32"] * world, "f16_serving_vs_fp32_plain": sat["f16"] / (rate32 / world),
-            "f16_serving_vs_f16_plain": sat["f16"] / (rate16 / world)}
+            "f16_serving_vs_f16_plain": sat["f16"] / (rate16 / world),
+            "cell_sorted_batches": {"f16_evals_per_s": sat["f16_sorted"] * world,
+                                    "f32_evals_per_s": sat["f32_sorted"] * world}}
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:

@@ -124,7 +124,8 @@ class TableInfo(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("vgh", C.c_int), ("pos_f64", C.c_int), ("rule", C.c_int), ("use_graphs", C.c_int),
-                ("max_inflight", C.c_int), ("max_batch_points", C.c_int), ("hbm_budget_bytes", C.c_uint64)]
+                ("max_inflight", C.c_int), ("max_batch_points", C.c_int), ("hbm_budget_bytes", C.c_uint64),
+                ("sort", C.c_int)]
 
 
 class ServerStats(C.Structure):

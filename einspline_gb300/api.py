@@ -406,12 +406,12 @@ class Server:
     """einspline_gb300_server_*: continuous batching of walker requests."""
 
     def __init__(self, spline: MultiUBspline3D, vgh=True, pos_f64=True, rule=0, use_graphs=True,
-                 max_inflight=3, max_batch_points=16384, hbm_budget_bytes=0):
+                 max_inflight=3, max_batch_points=16384, hbm_budget_bytes=0, sort=False):
         self.spline = spline
         self.pos_f64 = pos_f64
         self.vgh = vgh
         o = L.ServerOpts(int(vgh), int(pos_f64), rule, int(use_graphs), max_inflight, max_batch_points,
-                         hbm_budget_bytes)
+                         hbm_budget_bytes, int(sort))
         self.h = _lib().einspline_gb300_server_create(spline.table, C.byref(o))
         check()
         if not self.h:

@@ -89,6 +89,7 @@ struct Slot {
   Server *srv = nullptr;
   cudaStream_t stream = nullptr;
   char *stage_h = nullptr, *stage_d = nullptr;
+  void *sort_d = nullptr;      // counting-sort scratch (sort option)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaGraphNode_t n_copy = nullptr, n_kernel = nullptr, n_event = nullptr;
@@ -259,6 +260,11 @@ static int launch_batch(Server *v, Slot &s) {
     count_launch();
   } else {
     EG_CUDA(cudaMemcpyAsync(s.stage_d, s.stage_h, bytes, cudaMemcpyHostToDevice, s.stream));
+    if (v->o.sort && n > 1) {
+      int *perm = nullptr;
+      if (int r = small_sort_into(a, s.sort_d, &perm, s.stream)) return r;
+      a.perm = perm;
+    }
     if (int r = launch_eval(v->t, a, v->o.vgh != 0, s.stream, v->tx, v->ty, v->pb)) return r;
     EG_CUDA(cudaEventRecord(s.done, s.stream));
   }
@@ -381,6 +387,14 @@ einspline_gb300_server *einspline_gb300_server_create(einspline_gb300_table *t, 
   if (v->o.max_inflight <= 0) v->o.max_inflight = 3;
   v->o.max_inflight = std::min(v->o.max_inflight, 8);
   if (v->o.max_batch_points <= 0) v->o.max_batch_points = 16384;
+  if (v->o.sort) {
+    if (v->o.max_batch_points > kSmallSort) {
+      delete v;
+      fail(EINSPLINE_GB300_EINVAL, "server: sort takes max_batch_points <= %lld", (long long)kSmallSort);
+      return nullptr;
+    }
+    v->o.use_graphs = 0;  // the per-batch sort is launched directly
+  }
   v->rb = t->storage == ST_F64 ? 8 : 4;
   v->pos_b = v->o.pos_f64 ? 24 : 12;
   v->out_reals_per_pt = (v->o.vgh ? 10 : 1) * t->ncol;
@@ -403,14 +417,15 @@ einspline_gb300_server *einspline_gb300_server_create(einspline_gb300_table *t, 
   if (cudaMalloc(&v->arena_d, budget) != cudaSuccess) return bail("server arena");
   v->arena.reset(budget);
   v->st.budget_bytes = budget;
-  pick_tile(t, v->o.vgh != 0, v->o.max_batch_points, v->tx, v->ty, v->pb);
+  pick_tile(t, v->o.vgh != 0, v->o.max_batch_points, v->tx, v->ty, v->pb, v->o.sort != 0);
   v->slots.resize(v->o.max_inflight);
   for (auto &s : v->slots) {
     s.srv = v;
     if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMallocHost(&s.stage_h, v->stage_bytes()) != cudaSuccess ||
         cudaMalloc(&s.stage_d, v->stage_bytes()) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess ||
+        (v->o.sort && cudaMalloc(&s.sort_d, small_sort_bytes(v->o.max_batch_points)) != cudaSuccess))
       return bail("server slot");
     if (v->o.use_graphs && build_graph(v, s)) return bail("server graph");
   }
@@ -468,6 +483,7 @@ void destroy_server(Server *v) {
     if (sl.graph) cudaGraphDestroy(sl.graph);
     if (sl.stage_h) cudaFreeHost(sl.stage_h);
     if (sl.stage_d) cudaFree(sl.stage_d);
+    if (sl.sort_d) cudaFree(sl.sort_d);
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   cudaFree(v->arena_d);

@@ -227,6 +227,11 @@ typedef struct {
                                 largest request accepted */
   uint64_t hbm_budget_bytes; /* device memory for request outputs; 0 = 4 GiB
                                 or half of the free memory, whichever is less */
+  int sort;                  /* 1: visit each batch's points in cell order (a
+                                counting sort per batch, in scratch of each
+                                slot; batches are then launched without
+                                graphs; max_batch_points <= 131072); results
+                                are bit-identical to sort = 0 */
 } einspline_gb300_server_opts;
 
 /* Output layout per request: vals [npts][N], grads [npts][N][3],

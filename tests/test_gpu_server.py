@@ -21,11 +21,13 @@ def make_spline(kind="s", N=96, M=20, storage=api.STORE_NATIVE):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("use_graphs", [True, False])
-def test_alone_equals_in_mix(use_graphs):
+@pytest.mark.parametrize("use_graphs,sort", [(True, False), (False, False), (True, True)])
+def test_alone_equals_in_mix(use_graphs, sort):
+    """(sort: each batch visited in cell order, with its own sort scratch per
+    in-flight slot; the results are the same bits.)"""
     import torch
     G = make_spline()
-    S = api.Server(G, use_graphs=use_graphs, max_inflight=3, max_batch_points=2048)
+    S = api.Server(G, use_graphs=use_graphs, max_inflight=3, max_batch_points=2048, sort=sort)
     probe = synth.points_uniform(62, 300)
     rid = S.submit(probe)
     S.wait(rid)
