@@ -213,6 +213,7 @@ def _signatures():
     sig["einspline_gb300_set_load_mode"] = ([vp, i32], i32)
     sig["einspline_gb300_get_load_mode"] = ([vp], i32)
     sig["einspline_gb300_wait_status"] = ([vp], i32)
+    sig["einspline_gb300_test_wait_timeout"] = ([vp, i32, dbl], i32)
     sig["einspline_gb300_launch_count"] = ([], i64)
     sig["einspline_gb300_fill_uniform"] = ([vp, i64, i32, C.c_uint64, i64, dbl, dbl, vp], i32)
     sig["einspline_gb300_det_ratio"] = ([vp, C.POINTER(DetOpts), i32, vp, vp, vp, vp, vp, vp, vp], i32)

@@ -193,6 +193,16 @@ int small_sort_into(const EvalArgs &a, void *scratch, int **perm_out, cudaStream
   return 0;
 }
 
+// With CUDA's lazy module loading a kernel's code is brought to the device
+// on its first launch; asking for its attributes brings it there now.
+int load_sort_kernels() {
+  cudaFuncAttributes fa;
+  EG_CUDA(cudaFuncGetAttributes(&fa, k_cell_keys));
+  EG_CUDA(cudaFuncGetAttributes(&fa, k_sort_keys));
+  EG_CUDA(cudaFuncGetAttributes(&fa, k_sort_scatter));
+  return 0;
+}
+
 int sort_points(Table *t, const EvalArgs &a, int **perm_out, cudaStream_t s) {
   const int64_t n = a.npts;
   if (n > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "sorted evaluation takes at most %d points", INT_MAX);
@@ -344,7 +354,14 @@ int einspline_gb300_set_fp64_mode(einspline_gb300_table *t, int mode) {
       return 0;
     }
   }
-  return table_df_refresh(t);
+  if (int r = table_df_refresh(t)) {
+    // No double-float copy (its allocation failed): the table stays in IEEE
+    // mode, so no later flush tries to allocate the copy again.
+    std::lock_guard<std::mutex> lock(t->mu);
+    if (!t->df_coefs) t->fp64_mode = 0;
+    return r;
+  }
+  return 0;
 }
 
 int einspline_gb300_get_fp64_mode(einspline_gb300_table *t) {
@@ -450,6 +467,20 @@ int einspline_gb300_wait_status(einspline_gb300_table *t) {
   clear();
   if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
   return wait_status(t, "einspline_gb300_wait_status");
+}
+
+int einspline_gb300_test_wait_timeout(einspline_gb300_table *t, int stage, double seconds) {
+  clear();
+  if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
+  if (stage < 0) {
+    t->test_skip.store(0);
+    return 0;
+  }
+  if (!(seconds >= 1e-6 && seconds <= 1.0))
+    return fail(EINSPLINE_GB300_EINVAL, "the wait limit must lie in [1 us, 1 s] (got %g s)", seconds);
+  t->test_wait_ns = (unsigned long long)(seconds * 1e9);
+  t->test_skip.store(stage + 1);
+  return 0;
 }
 
 int einspline_gb300_set_tile(einspline_gb300_table *t, int tx, int ty, int pb) {

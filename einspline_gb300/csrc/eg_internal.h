@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 #include <unordered_map>
 #include <vector>
@@ -112,9 +113,10 @@ struct einspline_gb300_table {
   size_t factor_off[3] = {0, 0, 0};
   cudaStream_t stream = nullptr;
 
-  // single-point entry scratch
-  void *pt_dev = nullptr;           // device, 40 * ncol output reals
-  void *pt_host = nullptr;          // pinned host copy
+  // single-point entry scratch: 40 * ncol output reals in mapped pinned
+  // host memory, which the kernels write directly
+  void *pt_host = nullptr;
+  void *pt_dev = nullptr;           // its device address
 
   // host-buffer pipeline scratch (einspline_gb300_eval_3d_host)
   void *pipe_dev = nullptr;
@@ -135,6 +137,11 @@ struct einspline_gb300_table {
   // set by a TMA-staged evaluation whose bounded barrier wait ran out
   // (mapped pinned host word and its device address)
   int *wait_err_h = nullptr, *wait_err_d = nullptr;
+  // test hook for the next mode-4 launch (einspline_gb300_test_wait_timeout):
+  // the stage block 0 leaves without copies, plus one (0: off), and the
+  // launch's wait limit
+  std::atomic<int> test_skip{0};
+  unsigned long long test_wait_ns = 0;
   int tuned_tx[2] = {0, 0}, tuned_ty[2] = {0, 0}, tuned_pb[2] = {0, 0}, tuned_mode[2] = {0, 0};
   // the same for launches that visit points in cell order (sorted batches)
   int tuned_s_tx[2] = {0, 0}, tuned_s_ty[2] = {0, 0}, tuned_s_pb[2] = {0, 0}, tuned_s_mode[2] = {0, 0};
@@ -214,17 +221,23 @@ struct EvalArgs {
   const void *linv;           // out 1: 3x3 row-major G (output type)
   int64_t lrow;               // out 1: row stride of the gradient/laplacian rows (reals)
   int *wait_err;              // mode 4: set to 1 when a bounded barrier wait ran out
+  unsigned long long wait_ns; // mode 4: limit of each bounded wait (0: kWaitNs, 0.5 s)
+  int test_skip;              // mode 4 test hook: s + 1 makes block 0 issue no copy for
+                              // its stage s, so that stage's wait runs out (0: off)
   int box_bytes;              // mode 4: bytes of one box row (<= 256 stored reals)
   // mode 4: the table as a 4D tensor [x][y][z][column] (column innermost);
   // CUtensorMap is 128-byte aligned, and so is EvalArgs
   CUtensorMap tmap;
 };
 
-int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb);
+// mode >= 0 forces a load mode (EvalArgs::mode) instead of the table's choice.
+int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb, int mode = -1);
+// One point of a single-point entry (a.npts = 1, outputs in the point scratch).
+int launch_point(Table *t, EvalArgs &a, bool vgh);
 // ETIMEOUT (and clears the word) when a TMA-staged evaluation on t gave up a
 // bounded wait since the last check; call after the launches completed.
 int wait_status(Table *t, const char *fn);
-// Device and pinned host scratch of the single-point entries (40 * ncol reals).
+// Mapped pinned output scratch of the single-point entries (40 * ncol reals).
 int point_scratch(Table *t, const char *fn);
 void fill_eval_geometry(const Table *t, EvalArgs &a);
 // Kernel, grid, block and shared memory of a launch without launching it
@@ -248,5 +261,10 @@ size_t small_sort_bytes(int64_t n);
 int small_sort_into(const EvalArgs &a, void *scratch, int **perm_out, cudaStream_t s);
 // Morton key of each point's cell and its index (defined in api_ext.cu).
 __global__ void k_cell_keys(const EvalArgs a, uint64_t *keys, int *idx);
+// Bring kernels' code to the current device now rather than at their first
+// launch (CUDA loads modules lazily by default): the sort kernels, and the
+// evaluation kernel that a launch on t with these options would use.
+int load_sort_kernels();
+int load_eval_kernel(Table *t, bool vgh, bool sorted);
 
 }  // namespace eg

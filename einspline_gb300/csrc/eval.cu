@@ -413,9 +413,13 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
 
   // Thread 0 only: refill the buffer of stage q once every warp has released
   // its previous stage (q - NS).
+  const unsigned long long lim = a.wait_ns ? a.wait_ns : kWaitNs;
   auto produce = [&](int q) -> bool {
     const int slot = q % NS;
-    if (q >= NS && !mbar_wait(empty_s + 8 * slot, (unsigned)((q / NS - 1) & 1))) return false;
+    if (q >= NS && !mbar_wait(empty_s + 8 * slot, (unsigned)((q / NS - 1) & 1), lim)) return false;
+    // test hook: no arrival and no copy for this stage, so its full barrier
+    // never completes and the consumers' bounded wait runs out
+    if (a.test_skip == q + 1 && blockIdx.x == 0) return true;
     const int pp = q >> 2, i = q & 3;
     const unsigned full = full_s + 8 * slot;
     mbar_arrive_expect_tx(full, stage_bytes);
@@ -438,7 +442,7 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
       good = produce(issued);
       if (good) issued++;
     }
-    good = mbar_wait(full_s + 8 * (st % NS), (unsigned)((st / NS) & 1)) && good;
+    good = mbar_wait(full_s + 8 * (st % NS), (unsigned)((st / NS) & 1), lim) && good;
     if (!__all_sync(0xffffffffu, good)) break;
     const int pp = st >> 2, i = st & 3;
     const A *w = sw + pp * 36;
@@ -484,7 +488,7 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
       __threadfence_system();
     }
     if (threadIdx.x == 0)
-      for (int q = st; q < issued; q++) mbar_wait(full_s + 8 * (q % NS), (unsigned)((q / NS) & 1));
+      for (int q = st; q < issued; q++) mbar_wait(full_s + 8 * (q % NS), (unsigned)((q / NS) & 1), lim);
   }
 }
 
@@ -742,11 +746,11 @@ static size_t max_smem_optin() {
 // run one point lane (ty = 1) and need their stage buffers raised above the
 // 48 KB default once per kernel.
 static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const void **func, dim3 *block,
-                        size_t *smem) {
+                        size_t *smem, int mode = -1) {
   if (tx < 32 || tx % 32 || ty < 1 || tx * ty > 256 || pb < 1 || pb > 64)
     return fail(EINSPLINE_GB300_EINVAL, "bad launch shape tx=%d ty=%d pb=%d", tx, ty, pb);
   a.pb = pb;
-  a.mode = pick_mode(t, vgh, a.perm != nullptr);
+  a.mode = mode >= 0 ? mode : pick_mode(t, vgh, a.perm != nullptr);
   const int ks = kernel_storage(t);
   if (a.mode >= 2 && ks == ST_F64) a.mode = 0;        // IEEE FP64 is FMA-bound: no pipeline variant
   if (a.mode == 3 && !is16(t->storage)) a.mode = 2;   // the wide variant is for 16-bit tables
@@ -836,12 +840,16 @@ static int64_t plan_groups(EvalArgs &a, const void *func, dim3 block, size_t sme
   return a.g_tail + (rest + a.pb_tail - 1) / a.pb_tail;
 }
 
-int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb) {
+int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty, int pb, int mode) {
   if (a.npts <= 0) return 0;
   const void *func;
   dim3 block;
   size_t smem;
-  if (int r = shape_launch(t, a, vgh, tx, ty, pb, &func, &block, &smem)) return r;
+  if (int r = shape_launch(t, a, vgh, tx, ty, pb, &func, &block, &smem, mode)) return r;
+  if (a.mode == 4 && t->test_skip.load(std::memory_order_relaxed)) {
+    a.test_skip = t->test_skip.exchange(0);
+    a.wait_ns = t->test_wait_ns;
+  }
   const int64_t blocks = plan_groups(a, func, block, smem) * a.ntiles;
   if (blocks > INT_MAX) return fail(EINSPLINE_GB300_ESIZE, "too many points in one call (%lld)", (long long)a.npts);
   cudaError_t e;
@@ -861,6 +869,23 @@ int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty,
   }
   count_launch();
   if (e != cudaSuccess) return cuda_check(e, "evaluation kernel launch");
+  return 0;
+}
+
+int load_eval_kernel(Table *t, bool vgh, bool sorted) {
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  fill_eval_geometry(t, a);
+  static const int one = 0;
+  if (sorted) a.perm = &one;  // only its presence matters: it selects the sorted launch shape
+  int tx, ty, pb;
+  pick_tile(t, vgh, 1, tx, ty, pb, sorted);
+  const void *func;
+  dim3 block;
+  size_t smem;
+  if (int r = shape_launch(t, a, vgh, tx, ty, pb, &func, &block, &smem)) return r;
+  cudaFuncAttributes fa;
+  EG_CUDA(cudaFuncGetAttributes(&fa, func));
   return 0;
 }
 
@@ -922,19 +947,32 @@ int wait_status(Table *t, const char *fn) {
   return 0;
 }
 
-// Device and pinned host scratch for the single-point entries: 40 output
-// reals per column (value, 3 gradient, 9 Hessian, 27 third-derivative).
+// Output scratch of the single-point entries: 40 output reals per column
+// (value, 3 gradient, 9 Hessian, 27 third-derivative) in pinned host memory
+// mapped into the device's address space.  The kernels write their outputs
+// there directly, so a call needs no device-to-host copy: after the stream
+// synchronises the host reads them in place.
 int point_scratch(Table *t, const char *fn) {
-  if (t->pt_dev) return 0;
+  if (t->pt_host) return 0;
   const size_t sz = 40 * (size_t)t->ncol * acc_bytes(t);
-  if (cudaMalloc(&t->pt_dev, sz) != cudaSuccess || cudaMallocHost(&t->pt_host, sz) != cudaSuccess) {
+  void *h = nullptr, *d = nullptr;
+  if (cudaHostAlloc(&h, sz, cudaHostAllocMapped) != cudaSuccess || cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess) {
     cudaGetLastError();
-    if (t->pt_dev) cudaFree(t->pt_dev);
-    t->pt_dev = nullptr;
-    t->pt_host = nullptr;
+    if (h) cudaFreeHost(h);
     return fail(EINSPLINE_GB300_ENOMEM, "%s: scratch allocation failed", fn);
   }
+  t->pt_host = h;
+  t->pt_dev = d;
   return 0;
+}
+
+// Launch shape of a single-point evaluation: one warp per block and as many
+// blocks as the columns need, so a wide table's point is spread over many
+// SMs; the stencil rows of the point are first asked of L2 with bulk
+// prefetches (load mode 1), all 64 at once, unless the table forces a mode.
+int launch_point(Table *t, EvalArgs &a, bool vgh) {
+  const int mode = t->tile_mode >= 0 ? t->tile_mode : 1;
+  return launch_eval(t, a, vgh, t->stream, 32, 1, 1, mode);
 }
 
 }  // namespace eg
@@ -964,7 +1002,6 @@ void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, 
   std::lock_guard<std::mutex> g(t->mu);
   const size_t rb = acc_bytes(t);
   const size_t n = (size_t)t->ncol;
-  const size_t bytes = (vgh ? 13 : 1) * n * rb;
   if (point_scratch(t, fn)) return;
   EvalArgs a;
   memset(&a, 0, sizeof(a));
@@ -978,13 +1015,9 @@ void eval_point(S *s, double x, double y, double z, V *vals, V *grads, V *hess, 
   a.vals = t->pt_dev;
   a.grads = (char *)t->pt_dev + n * rb;
   a.hess = (char *)t->pt_dev + 4 * n * rb;
-  const int VW = elems_per_thread(t);
-  int tx = ((int)((n + VW - 1) / VW) + 31) / 32 * 32;
-  if (tx > 256) tx = 256;
-  if (launch_eval(t, a, vgh, t->stream, tx, 1, 1)) return;
-  if (cudaMemcpyAsync(t->pt_host, t->pt_dev, bytes, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
-      cudaStreamSynchronize(t->stream) != cudaSuccess) {
-    cuda_check(cudaGetLastError(), fn);
+  if (launch_point(t, a, vgh)) return;
+  if (cudaError_t e = cudaStreamSynchronize(t->stream)) {
+    cuda_check(e, fn);
     return;
   }
   if (wait_status(t, fn)) return;
@@ -1020,9 +1053,8 @@ void eval_point_vghgh(S *s, double x, double y, double z, V *vals, V *grads, V *
   a.hess = (char *)t->pt_dev + 4 * n * rb;
   a.ghess = (char *)t->pt_dev + 13 * n * rb;
   if (launch_vghgh(t, a, t->stream)) return;
-  if (cudaMemcpyAsync(t->pt_host, t->pt_dev, 40 * n * rb, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
-      cudaStreamSynchronize(t->stream) != cudaSuccess) {
-    cuda_check(cudaGetLastError(), fn);
+  if (cudaError_t e = cudaStreamSynchronize(t->stream)) {
+    cuda_check(e, fn);
     return;
   }
   memcpy(vals, t->pt_host, n * rb);

@@ -532,8 +532,8 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned byt
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 // Waits until the phase of the given parity has completed; false when
-// kWaitNs of global time passed first.
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+// limit_ns of global time passed first.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, unsigned long long limit_ns = kWaitNs) {
   unsigned long long t0 = 0;
   for (unsigned n = 1;; n++) {
     unsigned done;
@@ -548,7 +548,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
     if ((n & 63) == 0) {
       const unsigned long long now = global_ns();
       if (n == 64) t0 = now;
-      else if (now - t0 > kWaitNs) return false;
+      else if (now - t0 > limit_ns) return false;
     }
   }
 }

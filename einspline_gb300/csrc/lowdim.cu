@@ -248,10 +248,9 @@ void eval_point_ld(S *s, int dims, double x, double y, V *vals, V *grads, V *lh,
   a.grads = (char *)t->pt_dev + n * rb;
   a.hess = (char *)t->pt_dev + (1 + ng) * n * rb;
   if (launch_ld(t, a, t->stream)) return;
-  const size_t bytes = (1 + (form >= 1 ? ng : 0) + (form >= 2 ? nh : 0)) * n * rb;
-  if (cudaMemcpyAsync(t->pt_host, t->pt_dev, bytes, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
-      cudaStreamSynchronize(t->stream) != cudaSuccess) {
-    cuda_check(cudaGetLastError(), fn);
+  // the kernel wrote into the mapped host scratch directly
+  if (cudaError_t e = cudaStreamSynchronize(t->stream)) {
+    cuda_check(e, fn);
     return;
   }
   memcpy(vals, t->pt_host, n * rb);

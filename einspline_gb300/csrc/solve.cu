@@ -535,8 +535,7 @@ void table_destroy(Table *t) {
   cudaFree(t->scale);
   cudaFree(t->df_coefs);
   cudaFree(t->factors_d);
-  cudaFree(t->pt_dev);
-  if (t->pt_host) cudaFreeHost(t->pt_host);
+  if (t->pt_host) cudaFreeHost(t->pt_host);  // pt_dev is its device address
   if (t->wait_err_h) cudaFreeHost(t->wait_err_h);
   cudaFree(t->pipe_dev);
   cudaFree(t->sort_dev);

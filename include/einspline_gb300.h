@@ -153,11 +153,19 @@ int einspline_gb300_set_host_direct(einspline_gb300_table *t, int mode);
  * synchronisation cudaMalloc/cudaFree may cause.  The sort scratch is a fixed
  * 10 MiB file-scope device array that every GPU loading the library holds
  * until the process exits; npts above 262,144 is refused with ESIZE.  The
- * first call on a device looks the array's device address up
- * (cudaGetSymbolAddress), so make it before any stream capture.  All calls
- * share the array: calls that overlap on the GPU (different streams or
- * threads without ordering between them) race and must be serialised.
- * Results are bit-identical to einspline_gb300_eval_3d with sorting. */
+ * first call on a device (per CUDA context) is its set-up: it looks the
+ * array's device address up (cudaGetSymbolAddress) and loads this entry's
+ * kernels.  CUDA loads modules lazily by default, so this first call is when
+ * the 10 MiB array and the kernels' code take device memory: make it before
+ * a pool allocator takes the device's free memory, and before any stream
+ * capture.  An empty call (npts = 0) with the table and options of later
+ * calls does the whole set-up and nothing else.  A call may synchronise the
+ * table's stream when set_* calls are still queued (their solve runs
+ * first); an FP64 table in double-float mode whose double-float copy is
+ * missing is refused (ENOMEM) rather than given one.  All calls share the
+ * array: calls that overlap on the GPU (different streams or threads
+ * without ordering between them) race and must be serialised.  Results are
+ * bit-identical to einspline_gb300_eval_3d with sorting. */
 int einspline_gb300_eval_3d_sorted_noalloc(einspline_gb300_table *t, const einspline_gb300_eval_opts *opts,
                                            int64_t npts, const void *pos_d, void *vals_d, void *grads_d,
                                            void *hess_d, void *stream);
@@ -190,6 +198,16 @@ int einspline_gb300_get_load_mode(einspline_gb300_table *t);
  * after the launches have completed (synchronised stream).  The blocking
  * entries (single-point, host-buffer) check it themselves. */
 int einspline_gb300_wait_status(einspline_gb300_table *t);
+/* Testing the bounded waits without a fault: the next mode-4 launch on t
+ * has its first block issue no copy for its stage `stage` (stages count a
+ * block's point x-planes from 0), and every wait of that launch gives up
+ * after `seconds` (1 us .. 1 s) instead of 0.5 s.  That stage's barrier
+ * then never completes, its wait runs out, the block stops early and the
+ * launch reports ETIMEOUT through einspline_gb300_wait_status; no copy is
+ * left in flight and the next launch is unaffected.  Applies to one launch
+ * only; stage < 0 cancels it.  No counterpart in the reference, which
+ * aborts on a CUDA error instead. */
+int einspline_gb300_test_wait_timeout(einspline_gb300_table *t, int stage, double seconds);
 /* Time every candidate tile in every load mode on this table for npts
  * random points and keep the fastest (for vgh when vgh != 0); the choice is
  * cached per table. */

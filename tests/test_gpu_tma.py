@@ -150,3 +150,45 @@ def test_tma_mode_arguments():
     with pytest.raises(api.EinsplineError):
         G.set_load_mode(5)
     G.wait_status()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16])
+def test_tma_bounded_wait_runs_out_and_reports(storage):
+    """A wait that runs out, made without a fault: through the test hook the
+    first block of one launch issues no copy for its stage 1, so that stage's
+    barrier never completes.  With the wait limit shortened to 2 ms the
+    launch must end by itself, report ETIMEOUT through
+    einspline_gb300_wait_status (once: the status is cleared by reading it),
+    leave the context usable, and the next launch on the same table must be
+    clean and bit-identical to the copy-pipeline results."""
+    import torch
+    from einspline_gb300 import _lib as L
+    lib = L.load()
+    G = api.MultiUBspline3D("s", [(0.0, 1.0, 16)] * 3, [(P, P)] * 3, 256, storage=storage)
+    data = synth.grid_data_uniform(641, (16, 16, 16), 256, np.float32)
+    for i in range(256):
+        G.set(i, data[i])
+    G.flush()
+    pt = tpos(synth.points_uniform(642, 3000))
+    base = run(G, pt, 2, (64, 1, 8))
+    G.set_load_mode(4)
+    G.set_tile(64, 1, 8)
+    assert lib.einspline_gb300_test_wait_timeout(G.table, 1, 0.002) == 0
+    G.eval(pt, rule=0, layout=0)
+    torch.cuda.synchronize()
+    assert lib.einspline_gb300_wait_status(G.table) == 6  # EINSPLINE_GB300_ETIMEOUT
+    assert b"bounded wait" in lib.einspline_gb300_last_error_message()
+    lib.einspline_gb300_clear_error()
+    assert lib.einspline_gb300_wait_status(G.table) == 0
+    # the hook applied to one launch only: the next one completes, bit-identical
+    again = run(G, pt, 4, (64, 1, 8))
+    same(again, base, "after the timed-out launch")
+    assert lib.einspline_gb300_wait_status(G.table) == 0
+    # a cancelled hook leaves the next launch alone
+    assert lib.einspline_gb300_test_wait_timeout(G.table, 1, 0.002) == 0
+    assert lib.einspline_gb300_test_wait_timeout(G.table, -1, 0.0) == 0
+    same(run(G, pt, 4, (64, 1, 8)), base, "cancelled hook")
+    with pytest.raises(api.EinsplineError):
+        lib.einspline_gb300_test_wait_timeout(G.table, 1, 5.0)
+        L.check()

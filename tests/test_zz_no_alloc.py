@@ -5,7 +5,9 @@ run (their own pool allocator owns the device memory, or an allocation's
 implicit synchronisation would break their timing or capture).  It must give
 the same results as the allocating entry, einspline_gb300_eval_3d with
 sorting, through the C-ABI, on consecutive calls that share its fixed
-scratch array.  This file is collected last on purpose."""
+scratch array; after its set-up (an empty warm-up call) no call may take
+device memory, up to the largest batch it accepts.  This file is collected
+last on purpose."""
 import ctypes as C
 
 import numpy as np
@@ -14,12 +16,14 @@ import pytest
 from einspline_gb300 import _lib as L
 from einspline_gb300 import api, synth
 
-from helpers import TOL, rel_err
+from helpers import TOL
+
+MAX_POINTS = 262144  # the entry's fixed limit
 
 
-def _call(lib, G, opts, pos, out):
-    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
-    return lib.einspline_gb300_eval_3d_sorted_noalloc(G.table, C.byref(opts), pos.shape[0], ptr(pos), ptr(out[0]),
+def _call(lib, G, opts, npts, pos, out):
+    ptr = lambda t: C.c_void_p(t.data_ptr() if t is not None else 0)  # noqa: E731
+    return lib.einspline_gb300_eval_3d_sorted_noalloc(G.table, C.byref(opts), npts, ptr(pos), ptr(out[0]),
                                                       ptr(out[1]), ptr(out[2]), None)
 
 
@@ -37,25 +41,33 @@ def test_noalloc_sorted_matches_allocating_entry(kind):
     G.flush()
     dt = torch.float32 if kind == "s" else torch.float64
     opts = L.EvalOpts(1, 1, 0, 0, 1, 0, 0, 0)
-    # two calls in a row share the scratch (counting sort), then a batch large
-    # enough for the radix sort in the same scratch
-    for call, (seed, n) in enumerate(((11, 5000), (12, 5037), (13, 140000))):
-        pos = torch.from_numpy(synth.points_uniform(seed, n)).cuda()
-        P = pos.shape[0]
-        ref = G.eval(pos, vgh=True, rule=0, layout=0, sort=True)
-        out = (torch.full((P, N), -1.0, dtype=dt, device="cuda"), torch.full((P, N, 3), -1.0, dtype=dt, device="cuda"),
-               torch.full((P, N, 6), -1.0, dtype=dt, device="cuda"))
-        torch.cuda.synchronize()
-        free0 = torch.cuda.mem_get_info()[0]
-        rc = _call(lib, G, opts, pos, out)
+    # two calls in a row share the scratch (counting sort), then batches
+    # large enough for the radix sort in the same scratch, the last one at
+    # the entry's limit (the sort's largest work space)
+    cases = ((11, 5000), (12, 5037), (13, 140000), (14, MAX_POINTS))
+    pos, ref, out = [], [], []
+    for seed, n in cases:
+        p = torch.from_numpy(synth.points_uniform(seed, n)).cuda()
+        pos.append(p)
+        ref.append(G.eval(p, vgh=True, rule=0, layout=0, sort=True))
+        out.append((torch.full((n, N), -1.0, dtype=dt, device="cuda"),
+                    torch.full((n, N, 3), -1.0, dtype=dt, device="cuda"),
+                    torch.full((n, N, 6), -1.0, dtype=dt, device="cuda")))
+    torch.cuda.synchronize()
+    # set-up: an empty call with the options of the calls below
+    assert _call(lib, G, opts, 0, None, (None, None, None)) == 0, lib.einspline_gb300_last_error_message()
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for (seed, n), p, o in zip(cases, pos, out):
+        rc = _call(lib, G, opts, n, p, o)
         torch.cuda.synchronize()
         assert rc == 0, lib.einspline_gb300_last_error_message()
-        if call == 1:  # set-up is done: the second call must not take device memory
-            assert torch.cuda.mem_get_info()[0] == free0
-        for a, b in zip(out, ref):
-            a, b = a.cpu().numpy(), b.cpu().numpy()
-            assert rel_err(a, b) <= TOL[kind]
-            assert np.array_equal(a, b)
+        assert torch.cuda.mem_get_info()[0] == free0, f"call with {n} points took device memory"
+    for (seed, n), o, r in zip(cases, out, ref):
+        for a, b in zip(o, r):
+            den = float(b.abs().max())
+            assert float((a - b).abs().max()) / den <= TOL[kind]
+            assert torch.equal(a, b), f"{n} points: not bit-identical to the allocating entry"
 
 
 @pytest.mark.gpu
@@ -65,7 +77,7 @@ def test_noalloc_refuses_batches_beyond_its_scratch():
     G = api.MultiUBspline3D("s", [(0.0, 1.0, 8)] * 3, [(api.PERIODIC, api.PERIODIC)] * 3, 4)
     G.set(0, np.zeros((8, 8, 8), np.float32))
     opts = L.EvalOpts(0, 1, 0, 0, 1, 0, 0, 0)
-    n = 262145
+    n = MAX_POINTS + 1
     pos = torch.zeros((n, 3), dtype=torch.float64, device="cuda")
     v = torch.empty((n, 4), device="cuda")
     rc = lib.einspline_gb300_eval_3d_sorted_noalloc(G.table, C.byref(opts), n, C.c_void_p(pos.data_ptr()),
