@@ -38,6 +38,11 @@ _SIG = {"s": "Pf6float3S_PS_S1_S1_5uint3S2_i", "c": "Pf6float3S_PS_S1_S1_5uint3S
         "d": "Pd7double3S_PS_S1_S1_5uint3S2_i"}
 VGH_NAMES = {k: tuple(f"{p}41eval_multi_multi_UBspline_3d_{k}_vgh_kernel{sig}".encode() for p in ("_ZL", "_Z"))
              for k, sig in _SIG.items()}
+# The s vgl kernel (src/multi_bspline_cuda_s_impl.h:566-734): (float *pos,
+# float3 drInv, float *coefs, float Linv[], float *vals[], float *grad_lapl[],
+# uint3 dim, uint3 strides, int N, int row_stride).
+VGL_NAMES = tuple(f"{p}41eval_multi_multi_UBspline_3d_s_vgl_kernelPf6float3S_S_PS_S1_5uint3S2_ii".encode()
+                  for p in ("_ZL", "_Z"))
 BLOCK = 64  # SPLINE_BLOCK_SIZE of the reference's CUDA files
 
 
@@ -107,6 +112,12 @@ class RefVgh:
                     break
             else:
                 raise RuntimeError(f"the {kind} vgh kernel is not in the reference's device module")
+        self.vgl = None
+        for name in VGL_NAMES:
+            fn = C.c_void_p()
+            if cu.cuModuleGetFunction(C.byref(fn), self.mod, name) == 0:
+                self.vgl = fn
+                break
         for sym, dt in ((b"Acuda", np.float32), (b"Bcuda", np.float64)):
             dptr, nbytes = C.c_uint64(), C.c_size_t()
             self._check(cu.cuModuleGetGlobal_v2(C.byref(dptr), C.byref(nbytes), self.mod, sym), sym.decode())
@@ -139,5 +150,26 @@ class RefVgh:
         cols = 2 * n if kind == "c" else n  # the complex kernel runs over re/im columns
         gx = (cols + BLOCK - 1) // BLOCK
         self._check(self.cu.cuLaunchKernel(self.fn[kind], C.c_uint(gx), C.c_uint(num), C.c_uint(1), C.c_uint(BLOCK),
+                                           C.c_uint(1), C.c_uint(1), C.c_uint(0), C.c_void_p(stream), args, None),
+                    "cuLaunchKernel")
+
+    def launch_vgl(self, pos_d: int, num: int, drinv, coefs_d: int, linv_d: int, vals_pp: int, gl_pp: int, dim,
+                   strides, n: int, row_stride: int, stream: int) -> None:
+        """One launch of the s vgl kernel as eval_multi_multi_UBspline_3d_s_vgl_cuda
+        does (src/multi_bspline_cuda_s_impl.h:736-756): grid (ceil(N/64), num),
+        64 threads; grad_lapl[i] holds 4 rows of row_stride floats."""
+        if self.vgl is None:
+            raise RuntimeError("the s vgl kernel is not in the reference's device module")
+        if not 0 < num <= 65535:
+            raise ValueError("the reference kernel takes 1..65535 points per launch (gridDim.y)")
+        a_pos, a_coefs, a_linv = C.c_uint64(pos_d), C.c_uint64(coefs_d), C.c_uint64(linv_d)
+        a_v, a_g = C.c_uint64(vals_pp), C.c_uint64(gl_pp)
+        a_dr = Float3(*[float(x) for x in drinv])
+        a_dim, a_st = UInt3(*[int(x) for x in dim]), UInt3(*[int(x) for x in strides])
+        a_n, a_rs = C.c_int(n), C.c_int(row_stride)
+        args = (C.c_void_p * 10)(*[C.cast(C.pointer(x), C.c_void_p) for x in
+                                   (a_pos, a_dr, a_coefs, a_linv, a_v, a_g, a_dim, a_st, a_n, a_rs)])
+        gx = (n + BLOCK - 1) // BLOCK
+        self._check(self.cu.cuLaunchKernel(self.vgl, C.c_uint(gx), C.c_uint(num), C.c_uint(1), C.c_uint(BLOCK),
                                            C.c_uint(1), C.c_uint(1), C.c_uint(0), C.c_void_p(stream), args, None),
                     "cuLaunchKernel")

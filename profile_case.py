@@ -6,8 +6,8 @@ runs the evaluation `--launches` times and prints the CUDA-event time of each.
 Everything it touches is a few GB, larger than L2, so DRAM counters of one
 launch mean what they mean in the benchmark.
 
-    python -m einspline_gb300.profile_case --storage f16 --launches 3
-    python -m einspline_gb300.profile_case --storage f16 --det 2048  # fused determinant ratio
+    python profile_case.py --storage f16 --launches 3
+    python profile_case.py --storage f16 --det 2048  # fused determinant ratio
 """
 from __future__ import annotations
 

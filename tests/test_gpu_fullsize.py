@@ -121,14 +121,19 @@ def test_complex_64cube_256_sorted(orc):
     check_nodes(G, "c", M, N, seed, 128, F32_VS_F64)
 
 
-# Value error against FP64 per storage: (max |dv| / max |v|, ||dv|| / ||v||).
-# FP16 keeps 11 significant bits of each coefficient; the B-spline
+# Error against FP64 per storage, over all 1024 splines at 4096 points:
+# (max |d| / max |ref|, ||d|| / ||ref||, max over points of ||d_p|| / ||ref_p||).
+# The last one, the relative error of the orbital vector one evaluation
+# produces, is the definition under which the FP16 table is held to the
+# 1e-3 value-error target; the global relative L2 error is held to it too.
+# FP16 keeps 11 significant bits of each coefficient, and the B-spline
 # coefficients of rough data are several times larger than the data, so its
-# worst case sits near 1e-3 of the largest value (bounded by 2.44e-4 times the
-# largest coefficient, up to 2e-3 of the largest value) while its relative L2 error
-# is 3-4 times smaller.  I16 (uniform 16-bit steps) is ten times tighter.
-STORAGE_TOL = {api.STORE_F32: (2e-5, 1e-5), api.STORE_F16: (2e-3, 1e-3), api.STORE_I16: (2e-4, 1e-4),
-               api.STORE_BF16: (1.5e-2, 1e-2)}
+# largest single error reaches 1.2-1.3e-3 of the largest value over 16M
+# samples (bounded by 2.44e-4 times the largest coefficient): the first
+# figure is a regression bound, not the target.  I16 (uniform 16-bit steps)
+# is ten times tighter on every figure.
+STORAGE_TOL = {api.STORE_F32: (2e-5, 1e-5, 2e-5), api.STORE_F16: (2e-3, 1e-3, 1e-3),
+               api.STORE_I16: (2e-4, 1e-4, 2e-4), api.STORE_BF16: (1.5e-2, 1e-2, 1.5e-2)}
 
 
 def rel_l2(a, b):
@@ -137,23 +142,58 @@ def rel_l2(a, b):
     return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16, api.STORE_I16, api.STORE_BF16])
-def test_serving_table_64cube_1024_errors_vs_fp64(orc, storage):
-    """multi_UBspline_3d_s, 64^3, 1024 splines: FP32 and 16-bit tables
-    against the FP64 solve and evaluation on sampled columns."""
+def point_rel_l2_max(a, b):
+    """Largest relative L2 error of a point's outputs over all splines."""
+    a = np.asarray(a, np.float64).reshape(a.shape[0], -1)
+    b = np.asarray(b, np.float64).reshape(b.shape[0], -1)
+    return float((np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)).max())
+
+
+SERVE_M, SERVE_N, SERVE_SEED, SERVE_PTS = (64, 64, 64), 1024, 404, 4096
+
+
+@pytest.fixture(scope="module")
+def serving_fp64(orc):
+    """FP64 outputs of every spline of the 64^3 x 1024 data (the float data
+    promoted) at SERVE_PTS points: the library's IEEE FP64 table, itself
+    checked here against the oracle's FP64 evaluation on sampled columns."""
     import torch
-    tol_max, tol_l2 = STORAGE_TOL[storage]
-    M, N, seed = (64, 64, 64), 1024, 404
-    G, grids = device_table("s", M, N, seed, storage=storage)
-    pos = synth.points_uniform(405, 512)
-    v, g, h = (x.cpu().numpy() for x in G.eval(torch.from_numpy(pos).cuda(), rule=0, layout=0))
+    M, N, seed = SERVE_M, SERVE_N, SERVE_SEED
+    grids = [(0.0, 1.0, m) for m in M]
+    D = api.MultiUBspline3D("d", grids, [(P, P)] * 3, N)
+    per = int(np.prod(M))
+    buf = torch.empty((128,) + M, dtype=torch.float32, device="cuda")
+    for f in range(0, N, 128):
+        api.fill_uniform(buf, seed, -1.0, 1.0, offset=f * per)
+        D.set_device(f, buf.double())
+    D.flush()
+    pos = synth.points_uniform(405, SERVE_PTS)
+    ref = [x.cpu().numpy() for x in D.eval(torch.from_numpy(pos).cuda(), rule=0, layout=0)]
     cols = list(range(0, N, 128))
     T = sampled_oracle(orc, "s", grids, M, seed, cols)
-    rv, rg, rh = cpu_to_gpu_layout("d", *T.eval(pos, sem=0))
-    for name, a, b in (("value", v[:, cols], rv), ("gradient", g[:, cols], rg), ("hessian", h[:, cols], rh)):
-        assert rel_err(a, b) <= tol_max, (name, rel_err(a, b))
-        assert rel_l2(a, b) <= tol_l2, (name, rel_l2(a, b))
+    sub = np.arange(0, SERVE_PTS, 32)
+    pin = cpu_to_gpu_layout("d", *T.eval(pos[sub], sem=0))
+    assert_close(tuple(r[sub][:, cols] for r in ref), pin, TOL["d"], "FP64 table vs the oracle")
+    del D, buf
+    torch.cuda.empty_cache()
+    return grids, pos, ref
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16, api.STORE_I16, api.STORE_BF16])
+def test_serving_table_64cube_1024_errors_vs_fp64(serving_fp64, storage):
+    """multi_UBspline_3d_s, 64^3, 1024 splines: FP32 and 16-bit tables
+    against FP64 over all splines at 4096 points."""
+    import torch
+    tol_max, tol_l2, tol_pt = STORAGE_TOL[storage]
+    grids, pos, ref = serving_fp64
+    M, N, seed = SERVE_M, SERVE_N, SERVE_SEED
+    G, _ = device_table("s", M, N, seed, storage=storage)
+    got = [x.cpu().numpy() for x in G.eval(torch.from_numpy(pos).cuda(), rule=0, layout=0)]
+    for name, a, b in zip(("value", "gradient", "hessian"), got, ref):
+        assert point_rel_l2_max(a, b) <= tol_pt, (name, "per-point relative L2", point_rel_l2_max(a, b))
+        assert rel_l2(a, b) <= tol_l2, (name, "relative L2", rel_l2(a, b))
+        assert rel_err(a, b) <= tol_max, (name, "max-normalised", rel_err(a, b))
     check_nodes(G, "s", M, N, seed, 64, max(tol_max, F32_VS_F64))
 
 
@@ -179,7 +219,30 @@ def test_large_table_128cube_2048_int64_offsets(orc):
     ref_c = cpu_to_gpu_layout("d", *T.eval(corner, sem=0))
     assert_close((vc[0].cpu().numpy()[:, cols], vc[1].cpu().numpy()[:, cols], vc[2].cpu().numpy()[:, cols]),
                  ref_c, 4 * F32_VS_F64, "128^3 corner")
-    del G
+
+    # The whole 4096-walker x 256-point step in one launch (the reference's
+    # entry caps a launch at 65,535 points): 1,048,576 points, 84 GB of
+    # outputs.  The gradients and Hessians of the last points sit past 2^32
+    # elements of their buffers; the last 4096 points are checked against
+    # the oracle on the sampled columns, and bit for bit against the same
+    # points evaluated alone, in random and in cell-sorted order.
+    P, last = 4096 * 256, 4096
+    big = torch.from_numpy(synth.points_uniform(507, P)).cuda()
+    bufs = (torch.empty((P, N), device="cuda"), torch.empty((P, N, 3), device="cuda"),
+            torch.empty((P, N, 6), device="cuda"))
+    assert (P - 1) * N * 6 > 2 ** 32
+    tail = big[P - last:]
+    alone = [x.cpu().numpy() for x in G.eval(tail, rule=0, layout=0)]
+    x = tail.cpu().numpy()
+    ref_t = cpu_to_gpu_layout("d", *T.eval(x, sem=0))
+    for sort in (False, True):
+        G.eval(big, rule=0, layout=0, sort=sort, out=bufs)
+        torch.cuda.synchronize()
+        got = [b[P - last:].cpu().numpy() for b in bufs]
+        for a, b in zip(got, alone):
+            assert np.array_equal(a, b), f"last points of the 1M-point launch (sort={sort}) differ from alone"
+        assert_close(tuple(g[:, cols] for g in got), ref_t, 4 * F32_VS_F64, f"1M-point launch tail (sort={sort})")
+    del bufs, big, tail, G
     torch.cuda.empty_cache()
 
 
