@@ -137,8 +137,7 @@ __global__ void __launch_bounds__(kDetThreads, kDetBlocksPerSM) k_det_ratio(cons
     if (st < S) issue(st);
     cp_async_commit();
   }
-  float o[10][VW];
-  zero_out<float, VW>(o);
+  float o[10][VW];  // assigned by each point's plane 0
   float wz[3][4];
   float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   float av[VW];
@@ -198,7 +197,6 @@ __global__ void __launch_bounds__(kDetThreads, kDetBlocksPerSM) k_det_ratio(cons
           if (row && col0 + e < d.n) row[col0 + e] = o[0][e];
         }
       }
-      zero_out<float, VW>(o);
       if (g == G - 1) {
 #pragma unroll
         for (int q = 0; q < 5; q++) {

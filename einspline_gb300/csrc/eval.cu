@@ -54,10 +54,19 @@ __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col
       const float4 s4 = *reinterpret_cast<const float4 *>(a.scale + col0 + 4 * c);
       sc[4 * c] = s4.x; sc[4 * c + 1] = s4.y; sc[4 * c + 2] = s4.z; sc[4 * c + 3] = s4.w;
     }
+    if constexpr (std::is_same<A, float>::value && VW % 2 == 0) {
+      // column pairs in one packed multiply each (the same IEEE products)
 #pragma unroll
-    for (int q = 0; q < (VGH ? 10 : 1); q++)
+      for (int q = 0; q < (VGH ? 10 : 1); q++)
 #pragma unroll
-      for (int e = 0; e < VW; e++) o[q][e] *= (A)sc[e];
+        for (int e = 0; e < VW; e += 2)
+          upk2(mul2(pk2(o[q][e], o[q][e + 1]), pk2(sc[e], sc[e + 1])), o[q][e], o[q][e + 1]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < (VGH ? 10 : 1); q++)
+#pragma unroll
+        for (int e = 0; e < VW; e++) o[q][e] *= (A)sc[e];
+    }
   }
   if (a.sign) {
     const A sg = reinterpret_cast<const A *>(a.sign)[src];
@@ -275,7 +284,7 @@ __global__ void __launch_bounds__(256) k_eval(const EvalArgs a) {
 // and row instead of 4 columns and 8 bytes.  Same arithmetic, same order as
 // k_eval.
 template <int ST, bool VGH, bool WIDE>
-__global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
+__device__ __forceinline__ void eval_pipe_body(const EvalArgs &a) {
   using A = typename CT<ST>::A;
   using Raw = typename CT<ST>::Raw;
   constexpr int VW = WIDE ? 2 * CT<ST>::VW : CT<ST>::VW;
@@ -307,16 +316,20 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
     const int pp = st >> 2, i = st & 3;
     const char *plane = cbase + (sidx[3 * pp] + i) * xsb + sidx[3 * pp + 1] * ysb + sidx[3 * pp + 2] * zsb;
     const unsigned dst = my + (unsigned)(st % NS) * slot_step;
+    if (RB == 16 && a.perm) {
 #pragma unroll
-    for (int r = 0; r < 16; r++) cp_async<RB>(dst + r * row_step, plane + (r >> 2) * ysb + (r & 3) * zsb);
+      for (int r = 0; r < 16; r++) cp_async_ca16(dst + r * row_step, plane + (r >> 2) * ysb + (r & 3) * zsb);
+    } else {
+#pragma unroll
+      for (int r = 0; r < 16; r++) cp_async<RB>(dst + r * row_step, plane + (r >> 2) * ysb + (r & 3) * zsb);
+    }
   };
 #pragma unroll
   for (int st = 0; st < NS - 1; st++) {
     if (st < S) issue(st);
     cp_async_commit();
   }
-  A o[10][VW];
-  zero_out<A, VW>(o);
+  A o[10][VW];  // assigned by each point's plane 0
   A wz[3][4];
   for (int st = 0; st < S; st++) {
     if (st + NS - 1 < S) issue(st + NS - 1);
@@ -352,9 +365,21 @@ __global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
       } else {
         epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
       }
-      zero_out<A, VW>(o);
     }
   }
+}
+
+template <int ST, bool VGH, bool WIDE>
+__global__ void __launch_bounds__(256) k_eval_pipe(const EvalArgs a) {
+  eval_pipe_body<ST, VGH, WIDE>(a);
+}
+
+// The double-float variant is held to 168 registers: three warps of a
+// sub-partition then fit its 16K registers (12 resident warps per SM), which
+// its dependency-bound reduction needs more than a few registers of slack.
+template <bool VGH>
+__global__ void __maxnreg__(168) k_eval_pipe_df(const EvalArgs a) {
+  eval_pipe_body<ST_DF, VGH, false>(a);
 }
 
 // Tensor-map pipeline: a stage is again one x-plane of one point, but the
@@ -432,8 +457,7 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
   if (threadIdx.x == 0)
     for (; issued < NS - 1 && issued < S; issued++) produce(issued);
 
-  A o[10][VW];
-  zero_out<A, VW>(o);
+  A o[10][VW];  // assigned by each point's plane 0
   A wz[3][4];
   int st = 0;
   for (; st < S; st++) {
@@ -478,7 +502,6 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
           epilogue<A, VW, VGH>(a, ssrc[pp], col0, o);
         }
       }
-      zero_out<A, VW>(o);
     }
   }
   if (st < S) {
@@ -532,17 +555,10 @@ __global__ void __launch_bounds__(128) k_eval_vghgh(const EvalArgs a) {
                      idx[1] * ysb + idx[2] * zsb;
   A o[20][VW];
 #pragma unroll
-  for (int q = 0; q < 20; q++)
-#pragma unroll
-    for (int e = 0; e < VW; e++) o[q][e] = A(0);
-#pragma unroll
   for (int i = 0; i < 4; i++) {
-    // y[0..5] as in reduce_plane; y[6..9] = b3c0, b2c1, b1c2, b0c3
+    // y[0..5] as in reduce_plane; y[6..9] = b3c0, b2c1, b1c2, b0c3.  As
+    // there, every sum starts with a product.
     A y[10][VW];
-#pragma unroll
-    for (int q = 0; q < 10; q++)
-#pragma unroll
-      for (int e = 0; e < VW; e++) y[q][e] = A(0);
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       A c[4][VW];
@@ -567,42 +583,21 @@ __global__ void __launch_bounds__(128) k_eval_vghgh(const EvalArgs a) {
         z3 = fmaT(c[1][e], w3[2][1], z3);
         z3 = fmaT(c[2][e], w3[2][2], z3);
         z3 = fmaT(c[3][e], w3[2][3], z3);
-        y[0][e] = fmaT(by, z0, y[0][e]);
-        y[1][e] = fmaT(dby, z0, y[1][e]);
-        y[2][e] = fmaT(d2by, z0, y[2][e]);
-        y[3][e] = fmaT(by, z1, y[3][e]);
-        y[4][e] = fmaT(dby, z1, y[4][e]);
-        y[5][e] = fmaT(by, z2, y[5][e]);
-        y[6][e] = fmaT(d3by, z0, y[6][e]);
-        y[7][e] = fmaT(d2by, z1, y[7][e]);
-        y[8][e] = fmaT(dby, z2, y[8][e]);
-        y[9][e] = fmaT(by, z3, y[9][e]);
+        const A yw[10] = {by, dby, d2by, by, dby, by, d3by, d2by, dby, by};
+        const A zz[10] = {z0, z0, z0, z1, z1, z2, z0, z1, z2, z3};
+#pragma unroll
+        for (int q = 0; q < 10; q++) y[q][e] = j == 0 ? yw[q] * zz[q] : fmaT(yw[q], zz[q], y[q][e]);
       }
     }
     const A ax = w[i], dax = w[4 + i], d2ax = w[8 + i], d3ax = w3[0][i];
+    // o[q] += x weight * y[r]: value, gradient, Hessian (as in reduce_plane),
+    // then xxx, xxy, xxz, xyy, xyz, xzz, yyy, yyz, yzz, zzz
+    const A xw[20] = {ax, dax, ax, ax, d2ax, dax, dax, ax, ax, ax, d3ax, d2ax, d2ax, dax, dax, dax, ax, ax, ax, ax};
+    constexpr int R[20] = {0, 0, 1, 3, 0, 1, 3, 2, 4, 5, 0, 1, 3, 2, 4, 5, 6, 7, 8, 9};
 #pragma unroll
-    for (int e = 0; e < VW; e++) {
-      o[0][e] = fmaT(ax, y[0][e], o[0][e]);
-      o[1][e] = fmaT(dax, y[0][e], o[1][e]);
-      o[2][e] = fmaT(ax, y[1][e], o[2][e]);
-      o[3][e] = fmaT(ax, y[3][e], o[3][e]);
-      o[4][e] = fmaT(d2ax, y[0][e], o[4][e]);
-      o[5][e] = fmaT(dax, y[1][e], o[5][e]);
-      o[6][e] = fmaT(dax, y[3][e], o[6][e]);
-      o[7][e] = fmaT(ax, y[2][e], o[7][e]);
-      o[8][e] = fmaT(ax, y[4][e], o[8][e]);
-      o[9][e] = fmaT(ax, y[5][e], o[9][e]);
-      o[10][e] = fmaT(d3ax, y[0][e], o[10][e]);  // xxx
-      o[11][e] = fmaT(d2ax, y[1][e], o[11][e]);  // xxy
-      o[12][e] = fmaT(d2ax, y[3][e], o[12][e]);  // xxz
-      o[13][e] = fmaT(dax, y[2][e], o[13][e]);   // xyy
-      o[14][e] = fmaT(dax, y[4][e], o[14][e]);   // xyz
-      o[15][e] = fmaT(dax, y[5][e], o[15][e]);   // xzz
-      o[16][e] = fmaT(ax, y[6][e], o[16][e]);    // yyy
-      o[17][e] = fmaT(ax, y[7][e], o[17][e]);    // yyz
-      o[18][e] = fmaT(ax, y[8][e], o[18][e]);    // yzz
-      o[19][e] = fmaT(ax, y[9][e], o[19][e]);    // zzz
-    }
+    for (int e = 0; e < VW; e++)
+#pragma unroll
+      for (int q = 0; q < 20; q++) o[q][e] = i == 0 ? xw[q] * y[R[q]][e] : fmaT(xw[q], y[R[q]][e], o[q][e]);
   }
   if (a.scale) {
 #pragma unroll
@@ -671,9 +666,12 @@ template <int ST, bool VGH>
 static const void *kernel_for(int mode) {
   if constexpr (ST != ST_F64) {
     if (mode == 4) return (const void *)k_eval_tma<ST, VGH>;
-    if (mode == 2 || (mode == 3 && ST == ST_DF)) return (const void *)k_eval_pipe<ST, VGH, false>;
-    if constexpr (ST != ST_DF)
+    if constexpr (ST == ST_DF) {
+      if (mode == 2 || mode == 3) return (const void *)k_eval_pipe_df<VGH>;
+    } else {
+      if (mode == 2) return (const void *)k_eval_pipe<ST, VGH, false>;
       if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
+    }
   }
   return (const void *)k_eval<ST, VGH>;
 }

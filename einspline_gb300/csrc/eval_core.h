@@ -251,7 +251,13 @@ __device__ __forceinline__ void upk2(dfl2 x, dfl &a, dfl &b) {
 }
 __device__ __forceinline__ dfl2 mul2(dfl2 a, dfl2 b) {
   const f32x2 p = mul2(a.h, b.h);
-  f32x2 e = fma2(a.h, b.h, neg2(p));
+  // the exact product error per lane as two scalar FMAs, whose negated
+  // addend costs nothing (a packed negation would be two integer operations)
+  float a0, a1, b0, b1, p0, p1;
+  upk2(a.h, a0, a1);
+  upk2(b.h, b0, b1);
+  upk2(p, p0, p1);
+  f32x2 e = pk2(fmaf(a0, b0, -p0), fmaf(a1, b1, -p1));
   e = fma2(a.h, b.l, e);
   e = fma2(a.l, b.h, e);
   return dfl2{p, e};
@@ -268,7 +274,8 @@ __device__ __forceinline__ dfl2 fma2(dfl2 a, dfl2 b, dfl2 c) {
 // w: [0..11] x weights, [12..23] y weights, [24..35] z weights.
 // o: v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz.
 // One x-plane i: rows (i, j, k) come from row(j, k, c); z first, then y,
-// then this plane's x terms are added to o.
+// then this plane's x terms go to o.  Every sum starts with a product (no
+// accumulator starts at zero): plane 0 assigns o, later planes add to it.
 template <typename A, int VW, bool VGH, typename RowFn>
 __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3][4], RowFn row, A (&o)[10][VW]) {
   if constexpr ((std::is_same<A, float>::value && VW % 2 == 0) || (std::is_same<A, dfl>::value && VW == 2)) {
@@ -281,10 +288,6 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
 #pragma unroll
       for (int k = 0; k < 4; k++) wz2[d][k] = pk2(wz[d][k], wz[d][k]);
     P y[6][H];
-#pragma unroll
-    for (int q = 0; q < 6; q++)
-#pragma unroll
-      for (int e = 0; e < H; e++) y[q][e] = pk2(A(0.f), A(0.f));
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       A c[4][VW];
@@ -299,7 +302,7 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
         z0 = fma2(c1, wz2[0][1], z0);
         z0 = fma2(c2, wz2[0][2], z0);
         z0 = fma2(c3, wz2[0][3], z0);
-        y[0][e] = fma2(by, z0, y[0][e]);
+        y[0][e] = j == 0 ? mul2(by, z0) : fma2(by, z0, y[0][e]);
         if (VGH) {
           P z1 = mul2(c0, wz2[1][0]);
           z1 = fma2(c1, wz2[1][1], z1);
@@ -309,35 +312,46 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
           z2 = fma2(c1, wz2[2][1], z2);
           z2 = fma2(c2, wz2[2][2], z2);
           z2 = fma2(c3, wz2[2][3], z2);
-          y[1][e] = fma2(dby, z0, y[1][e]);
-          y[2][e] = fma2(d2by, z0, y[2][e]);
-          y[3][e] = fma2(by, z1, y[3][e]);
-          y[4][e] = fma2(dby, z1, y[4][e]);
-          y[5][e] = fma2(by, z2, y[5][e]);
+          if (j == 0) {
+            y[1][e] = mul2(dby, z0);
+            y[2][e] = mul2(d2by, z0);
+            y[3][e] = mul2(by, z1);
+            y[4][e] = mul2(dby, z1);
+            y[5][e] = mul2(by, z2);
+          } else {
+            y[1][e] = fma2(dby, z0, y[1][e]);
+            y[2][e] = fma2(d2by, z0, y[2][e]);
+            y[3][e] = fma2(by, z1, y[3][e]);
+            y[4][e] = fma2(dby, z1, y[4][e]);
+            y[5][e] = fma2(by, z2, y[5][e]);
+          }
         }
       }
     }
     const P ax = pk2(w[i], w[i]), dax = pk2(w[4 + i], w[4 + i]), d2ax = pk2(w[8 + i], w[8 + i]);
+    // o[q] += x weight * y[r] for the ten (q, weight, r) of the scalar path
+    constexpr int R[10] = {0, 0, 1, 3, 0, 1, 3, 2, 4, 5};
+    constexpr int X[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
+    if (i == 0) {
 #pragma unroll
-    for (int e = 0; e < H; e++) {
-      // o[q] += x weight * y[r] for the ten (q, weight, r) of the scalar path
-      constexpr int R[10] = {0, 0, 1, 3, 0, 1, 3, 2, 4, 5};
-      constexpr int X[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
+      for (int e = 0; e < H; e++)
 #pragma unroll
-      for (int q = 0; q < (VGH ? 10 : 1); q++) {
-        const P xw = X[q] == 0 ? ax : (X[q] == 1 ? dax : d2ax);
-        P acc = pk2(o[q][2 * e], o[q][2 * e + 1]);
-        acc = fma2(xw, y[R[q]][e], acc);
-        upk2(acc, o[q][2 * e], o[q][2 * e + 1]);
-      }
+        for (int q = 0; q < (VGH ? 10 : 1); q++) {
+          const P xw = X[q] == 0 ? ax : (X[q] == 1 ? dax : d2ax);
+          upk2(mul2(xw, y[R[q]][e]), o[q][2 * e], o[q][2 * e + 1]);
+        }
+    } else {
+#pragma unroll
+      for (int e = 0; e < H; e++)
+#pragma unroll
+        for (int q = 0; q < (VGH ? 10 : 1); q++) {
+          const P xw = X[q] == 0 ? ax : (X[q] == 1 ? dax : d2ax);
+          upk2(fma2(xw, y[R[q]][e], pk2(o[q][2 * e], o[q][2 * e + 1])), o[q][2 * e], o[q][2 * e + 1]);
+        }
     }
     return;
   }
   A y[6][VW];
-#pragma unroll
-  for (int q = 0; q < 6; q++)
-#pragma unroll
-    for (int e = 0; e < VW; e++) y[q][e] = A(0);
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     A c[4][VW];
@@ -350,7 +364,7 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
       z0 = fmaT(c[1][e], wz[0][1], z0);
       z0 = fmaT(c[2][e], wz[0][2], z0);
       z0 = fmaT(c[3][e], wz[0][3], z0);
-      y[0][e] = fmaT(by, z0, y[0][e]);
+      y[0][e] = j == 0 ? by * z0 : fmaT(by, z0, y[0][e]);
       if (VGH) {
         A z1 = c[0][e] * wz[1][0];
         z1 = fmaT(c[1][e], wz[1][1], z1);
@@ -360,15 +374,41 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
         z2 = fmaT(c[1][e], wz[2][1], z2);
         z2 = fmaT(c[2][e], wz[2][2], z2);
         z2 = fmaT(c[3][e], wz[2][3], z2);
-        y[1][e] = fmaT(dby, z0, y[1][e]);
-        y[2][e] = fmaT(d2by, z0, y[2][e]);
-        y[3][e] = fmaT(by, z1, y[3][e]);
-        y[4][e] = fmaT(dby, z1, y[4][e]);
-        y[5][e] = fmaT(by, z2, y[5][e]);
+        if (j == 0) {
+          y[1][e] = dby * z0;
+          y[2][e] = d2by * z0;
+          y[3][e] = by * z1;
+          y[4][e] = dby * z1;
+          y[5][e] = by * z2;
+        } else {
+          y[1][e] = fmaT(dby, z0, y[1][e]);
+          y[2][e] = fmaT(d2by, z0, y[2][e]);
+          y[3][e] = fmaT(by, z1, y[3][e]);
+          y[4][e] = fmaT(dby, z1, y[4][e]);
+          y[5][e] = fmaT(by, z2, y[5][e]);
+        }
       }
     }
   }
   const A ax = w[i], dax = w[4 + i], d2ax = w[8 + i];
+  if (i == 0) {
+#pragma unroll
+    for (int e = 0; e < VW; e++) {
+      o[0][e] = ax * y[0][e];
+      if (VGH) {
+        o[1][e] = dax * y[0][e];
+        o[2][e] = ax * y[1][e];
+        o[3][e] = ax * y[3][e];
+        o[4][e] = d2ax * y[0][e];
+        o[5][e] = dax * y[1][e];
+        o[6][e] = dax * y[3][e];
+        o[7][e] = ax * y[2][e];
+        o[8][e] = ax * y[4][e];
+        o[9][e] = ax * y[5][e];
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int e = 0; e < VW; e++) {
     o[0][e] = fmaT(ax, y[0][e], o[0][e]);
@@ -386,14 +426,6 @@ __device__ __forceinline__ void reduce_plane(int i, const A *w, const A (&wz)[3]
   }
 }
 
-template <typename A, int VW>
-__device__ __forceinline__ void zero_out(A (&o)[10][VW]) {
-#pragma unroll
-  for (int q = 0; q < 10; q++)
-#pragma unroll
-    for (int e = 0; e < VW; e++) o[q][e] = A(0);
-}
-
 template <typename A>
 __device__ __forceinline__ void z_weights(const A *w, A (&wz)[3][4]) {
 #pragma unroll
@@ -408,7 +440,6 @@ __device__ __forceinline__ void contract(const char *base, int64_t xsb, int64_t 
                                          const typename CT<ST>::A *w, typename CT<ST>::A (&o)[10][CT<ST>::VW]) {
   using A = typename CT<ST>::A;
   constexpr int VW = CT<ST>::VW;
-  zero_out<A, VW>(o);
   A wz[3][4];
   z_weights<A>(w, wz);
 #pragma unroll 1
@@ -481,6 +512,11 @@ __device__ __forceinline__ void cp_async(unsigned dst, const char *src) {
   if constexpr (RB == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
   else if constexpr (RB == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
   else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+// The same 16-byte copy kept in L1 on its way: for launches that visit
+// points in cell order, where a block's consecutive points share stencil rows.
+__device__ __forceinline__ void cp_async_ca16(unsigned dst, const char *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
