@@ -106,14 +106,15 @@ template <> struct CT<ST_F64> {
 };
 
 // The double-float shadow of an FP64 table: (hi, lo) per coefficient, two
-// columns per 16-byte load.
+// columns per 16-byte load, stored as (hi0, hi1, lo0, lo1) so that the high
+// and the low parts of a column pair arrive as register pairs.
 template <> struct CT<ST_DF> {
   using A = dfl;
   using Raw = float4;
   static constexpr int VW = 2, BYTES = 8;
   __device__ static __forceinline__ void decode(const Raw &x, dfl (&v)[2]) {
-    v[0] = dfl(x.x, x.y);
-    v[1] = dfl(x.z, x.w);
+    v[0] = dfl(x.x, x.z);
+    v[1] = dfl(x.y, x.w);
   }
 };
 
@@ -512,11 +513,6 @@ __device__ __forceinline__ void cp_async(unsigned dst, const char *src) {
   if constexpr (RB == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
   else if constexpr (RB == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
   else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
-}
-// The same 16-byte copy kept in L1 on its way: for launches that visit
-// points in cell order, where a block's consecutive points share stencil rows.
-__device__ __forceinline__ void cp_async_ca16(unsigned dst, const char *src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>

@@ -659,12 +659,18 @@ static int flush_locked(Table *t, const AxisOverride *ov = nullptr) {
   return 0;
 }
 
-// Each FP64 coefficient as (hi, lo) = (round(c), round(c - hi)).
-__global__ void k_to_df(const double *__restrict__ c, float2 *__restrict__ out, int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double v = c[i];
-    const float h = __double2float_rn(v);
-    out[i] = make_float2(h, __double2float_rn(__dsub_rn(v, (double)h)));
+// Each FP64 coefficient as (hi, lo) = (round(c), round(c - hi)), stored per
+// pair of adjacent columns as (hi0, hi1, lo0, lo1): one 16-byte load then
+// gives the two high parts and the two low parts as the register pairs the
+// packed f32x2 arithmetic takes, with no moves to regroup them (n is even:
+// rows are padded to 128 bytes).
+__global__ void k_to_df(const double *__restrict__ c, float4 *__restrict__ out, int64_t n) {
+  const double2 *c2 = reinterpret_cast<const double2 *>(c);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n / 2; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = c2[i];
+    const float h0 = __double2float_rn(v.x), h1 = __double2float_rn(v.y);
+    out[i] = make_float4(h0, h1, __double2float_rn(__dsub_rn(v.x, (double)h0)),
+                         __double2float_rn(__dsub_rn(v.y, (double)h1)));
   }
 }
 
@@ -677,8 +683,8 @@ static int df_refresh_locked(Table *t) {
                 t->table_bytes);
   }
   const int64_t n = (int64_t)(t->table_bytes / sizeof(double));
-  k_to_df<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, t->stream>>>((const double *)t->coefs,
-                                                                                      (float2 *)t->df_coefs, n);
+  k_to_df<<<(unsigned)std::min<int64_t>((n / 2 + 255) / 256, 4096), 256, 0, t->stream>>>((const double *)t->coefs,
+                                                                                          (float4 *)t->df_coefs, n);
   count_launch();
   EG_CUDA(cudaGetLastError());
   EG_CUDA(cudaStreamSynchronize(t->stream));
