@@ -134,7 +134,8 @@ class MultiUBspline3D:
     def set_load_mode(self, mode: int) -> None:
         """0 direct loads, 1 L2 bulk prefetch, 2 shared-memory async pipeline,
         3 the same with 8 columns a thread (16-bit tables), 4 shared-memory
-        pipeline fed by tensor-map (TMA) copies, -1 autotuned."""
+        pipeline fed by tensor-map (TMA) copies, 5 tensor-core reduction (F16
+        tables; FP32-rounding agreement, not bit-identical), -1 autotuned."""
         _lib().einspline_gb300_set_load_mode(self.table, int(mode))
         check()
 

@@ -458,7 +458,7 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode) {
   clear();
   if (!table3_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "bad table handle");
-  if (mode < -1 || mode > 4) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1, 2, 3 or 4");
+  if (mode < -1 || mode > 5) return fail(EINSPLINE_GB300_EINVAL, "load mode must be -1, 0, 1, 2, 3, 4 or 5");
   t->tile_mode = mode;
   return 0;
 }

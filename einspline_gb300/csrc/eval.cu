@@ -45,10 +45,14 @@ __device__ __forceinline__ int h9to6(int m) {
   return (m == 0) ? 0 : (m == 1 || m == 3) ? 1 : (m == 2 || m == 6) ? 2 : (m == 4) ? 3 : (m == 5 || m == 7) ? 4 : 5;
 }
 
-template <typename A, int VW, bool VGH>
+template <typename A, int VW, bool VGH, bool SCALE = true>
 __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col0, A (&o)[10][VW]) {
-  if (a.scale) {
+  if (SCALE && a.scale) {
     float sc[VW];
+    if constexpr (VW % 4 != 0) {
+#pragma unroll
+      for (int e = 0; e < VW; e++) sc[e] = a.scale[col0 + e];
+    }
 #pragma unroll
     for (int c = 0; c < VW / 4; c++) {
       const float4 s4 = *reinterpret_cast<const float4 *>(a.scale + col0 + 4 * c);
@@ -76,7 +80,8 @@ __device__ __forceinline__ void epilogue(const EvalArgs &a, int64_t src, int col
       for (int e = 0; e < VW; e++) o[q][e] *= sg;
   }
   A *vp = a.vals_pp ? (A *)a.vals_pp[src] : (A *)a.vals + src * a.vstride;
-  const bool full = col0 + VW <= a.ncol;
+  // vector stores need whole 16-byte groups of columns in this thread
+  const bool full = (sizeof(A) == 8 ? VW % 2 == 0 : VW % 4 == 0) && col0 + VW <= a.ncol;
   {
     A v[VW];
 #pragma unroll
@@ -513,6 +518,246 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
   }
 }
 
+// Tensor-core evaluation (load mode 5, F16 tables).  For one point the ten
+// outputs of a column are a product of the point's 10 x 64 stencil weights
+// with the column's 64 stencil coefficients, so a block owns 128
+// consecutive columns and, point after point of its group, computes
+//   D[128 columns x 32] = A[128 columns x 64 rows] * B[64 rows x 32]
+// with four tcgen05.mma (M 128, N 32, K 16: one per x-plane) into an f32
+// accumulator in tensor memory.  A is the stencil exactly as stored: two TMA
+// boxes of 64 columns x 4 z x 4 y x 4 x, in the 128-byte swizzle, which is
+// the MN-major operand layout.  B holds each output's weights w_x w_y w_z
+// (computed in FP32 without the delta_inv factors) split into f16 high and
+// low parts, one column each: output q = D[2q] + D[2q+1], then times its
+// delta_inv factors, the spline's factor and the point's sign.  The
+// products of f16 coefficients with the 22-bit weights are exact and the
+// sums are FP32, so results agree with the FMA kernels to FP32 rounding
+// (not bit for bit).
+// Warp roles, synchronised only through mbarriers: warp 0 (one lane) keeps
+// the stencil copies of up to kTcStages points in flight; warp 1 (one lane)
+// issues each point's MMAs once its stencil, its weight matrix and a free
+// accumulator are there, and commits them to the barriers that free the
+// stage, the weight buffer and fill the accumulator; warps 2-5 (one column a
+// thread, each warp the TMEM lanes of its quarter) build the next point's
+// weight matrix, then read this point's accumulator and store its outputs.
+// Weight matrices and accumulators are double-buffered.  Every wait is
+// bounded and also ends when another role gave up (a shared flag): a block
+// that gave up sets a.wait_err, waits (again bounded) for its copies and
+// MMAs in flight, and frees its tensor memory.
+template <bool VGH>
+__global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ EvalArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NS = kTcStages;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tile = blockIdx.x % a.ntiles;
+  const int64_t grp = blockIdx.x / a.ntiles;
+  const int64_t p0 = group_first(a, grp);
+  float *sw = reinterpret_cast<float *>(smem);
+  int *sidx = reinterpret_cast<int *>(smem + smem_w_bytes(a.pb, 4));
+  int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, 4) + align_up((size_t)a.pb * 12, 8));
+  const int pn = (int)min((int64_t)group_cap(a, grp), a.npts - p0);
+  // cells and the unscaled basis weights (delta_inv applied to the outputs)
+  for (int q = tid; q < pn * 3; q += kTcThreads) {
+    const int pp = q / 3, ax = q - 3 * pp;
+    const int64_t src = a.perm ? (int64_t)a.perm[p0 + pp] : p0 + pp;
+    double xd;
+    if (!a.pos) xd = a.inl[ax];
+    else if (a.pos_f64) xd = reinterpret_cast<const double *>(a.pos)[3 * src + ax];
+    else xd = (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
+    int idx;
+    float t;
+    cell(a, ax, xd, idx, t);
+    bspline_weights<float>(t, sw + pp * 36 + ax * 12, 1.0f);
+    sidx[pp * 3 + ax] = idx;
+    if (ax == 0) ssrc[pp] = src;
+  }
+  const unsigned base_s = (unsigned)__cvta_generic_to_shared(smem);
+  const unsigned a_s = (base_s + (unsigned)smem_total(a.pb, 4) + 1023u) & ~1023u;
+  const unsigned b_s = a_s + NS * 16384u;
+  // mbarriers: full/empty per stage; weight matrix full/empty, accumulator
+  // full/empty per buffer; then the TMEM address, the abort flag and the
+  // count of points whose stencil the MMA warp consumed
+  const unsigned full_s = b_s + 2 * 4096u, empty_s = full_s + 8 * NS, bfull_s = empty_s + 8 * NS;
+  const unsigned bempty_s = bfull_s + 16, tfull_s = bempty_s + 16, tempty_s = tfull_s + 16, slot_s = tempty_s + 16;
+  unsigned char *bgen = smem + (b_s - base_s);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + (slot_s + 4 - base_s));
+  volatile int *consumed = reinterpret_cast<volatile int *>(smem + (slot_s + 8 - base_s));
+  // weight columns 20..31 (and all but 0, 1 for value only) stay zero
+  for (int e = tid; e < 2 * 4096 / 16; e += kTcThreads) reinterpret_cast<uint4 *>(bgen)[e] = make_uint4(0, 0, 0, 0);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(slot_s) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 32) {
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      mbar_init(full_s + 8 * s, 1);
+      mbar_init(empty_s + 8 * s, 1);
+    }
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      mbar_init(bfull_s + 8 * b, kTcCols);
+      mbar_init(bempty_s + 8 * b, 1);
+      mbar_init(tfull_s + 8 * b, 1);
+      mbar_init(tempty_s + 8 * b, kTcCols);
+    }
+    *abort_flag = 0;
+    *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *reinterpret_cast<volatile unsigned *>(smem + (slot_s - base_s));
+  const int c_first = tile * kTcCols;
+  const unsigned long long lim = a.wait_ns ? a.wait_ns : kWaitNs;
+  // a bounded wait that also gives up once another role has
+  auto wait = [&](unsigned bar, unsigned parity) -> bool {
+    if (*abort_flag) return false;
+    if (mbar_wait(bar, parity, lim)) return true;
+    *abort_flag = 1;
+    return false;
+  };
+  int issued = 0, skipped = -1, last_commit = -1;
+  if (warp == 0) {
+    if (lane == 0) {
+      // stencil copies
+      tma_prefetch_map(&a.tmap);
+      for (int p = 0; p < pn; p++) {
+        const int s = p % NS;
+        if (p >= NS && !wait(empty_s + 8 * s, (unsigned)((p / NS - 1) & 1))) break;
+        issued = p + 1;
+        // test hook: no copy for this point, so its wait runs out
+        if (a.test_skip == p + 1 && blockIdx.x == 0) { skipped = p; continue; }
+        mbar_arrive_expect_tx(full_s + 8 * s, 16384u);
+#pragma unroll
+        for (int mg = 0; mg < 2; mg++)
+          tma_load_4d(a_s + s * 16384u + mg * 8192u, &a.tmap, full_s + 8 * s, c_first + 64 * mg, sidx[3 * p + 2],
+                      sidx[3 * p + 1], sidx[3 * p]);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMAs
+      constexpr uint32_t idesc = umma_idesc_f16(kTcCols, kTcN);
+      for (int p = 0; p < pn; p++) {
+        const int s = p % NS, bb = p & 1;
+        if (!wait(full_s + 8 * s, (unsigned)((p / NS) & 1))) break;
+        *consumed = p + 1;
+        if (!wait(bfull_s + 8 * bb, (unsigned)((p >> 1) & 1))) break;
+        if (p >= 2 && !wait(tempty_s + 8 * bb, (unsigned)(((p >> 1) - 1) & 1))) break;
+        tc_fence_after();
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          umma_f16(tmem + bb * kTcN, umma_desc(a_s + s * 16384u + i * 2048u, 8192u, 1024u, 2),
+                   umma_desc(b_s + bb * 4096u + i * 1024u, 128u, 256u, 0), idesc, i > 0);
+        umma_commit(empty_s + 8 * s);
+        umma_commit(bempty_s + 8 * bb);
+        umma_commit(tfull_s + 8 * bb);
+        last_commit = p;
+      }
+    }
+  } else {
+    // weight matrices and outputs: thread et owns column c_first + colr
+    const int et = tid - 64;
+    const int colr = (warp & 3) * 32 + lane;
+    const int col = c_first + colr;
+    // this thread's share of a weight matrix: stencil row k, outputs 0-4
+    // (even threads) or 5-9 (odd threads)
+    const int k = et >> 1;
+    const int ki = k >> 4, kj = (k >> 2) & 3, km = k & 3, kk = k & 15;
+    const unsigned boff = ki * 1024 + (kk >> 3) * 128 + (kk & 7) * 2;
+    // derivative orders in x, y, z of each output (v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz)
+    static constexpr int OA[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
+    static constexpr int OB[10] = {0, 0, 1, 0, 0, 1, 0, 2, 1, 0};
+    static constexpr int OC[10] = {0, 0, 0, 1, 0, 0, 1, 0, 1, 2};
+    const float dx = a.dinvf[0], dy = a.dinvf[1], dz = a.dinvf[2];
+    const float sc = (a.scale && col < a.ncol) ? a.scale[col] : 1.f;
+    // Weight matrix of point p into buffer p & 1, then arrive on its barrier.
+    auto build_b = [&](int p) {
+      const float *w = sw + p * 36;
+      unsigned char *bm = bgen + (p & 1) * 4096 + boff;
+      // weight of output q at this row, as f16 high and low parts in columns 2q, 2q + 1
+      auto put = [&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        const float wq = w[OA[q] * 4 + ki] * w[12 + OB[q] * 4 + kj] * w[24 + OC[q] * 4 + km];
+        const __half hi = __float2half_rn(wq);
+        const __half lo = __float2half_rn(wq - __half2float(hi));
+        *reinterpret_cast<__half *>(bm + ((2 * q) >> 3) * 256 + ((2 * q) & 7) * 16) = hi;
+        *reinterpret_cast<__half *>(bm + ((2 * q + 1) >> 3) * 256 + ((2 * q + 1) & 7) * 16) = lo;
+      };
+      if (!(et & 1)) {
+        put(std::integral_constant<int, 0>());
+        if constexpr (VGH) {
+          put(std::integral_constant<int, 1>());
+          put(std::integral_constant<int, 2>());
+          put(std::integral_constant<int, 3>());
+          put(std::integral_constant<int, 4>());
+        }
+      } else if constexpr (VGH) {
+        put(std::integral_constant<int, 5>());
+        put(std::integral_constant<int, 6>());
+        put(std::integral_constant<int, 7>());
+        put(std::integral_constant<int, 8>());
+        put(std::integral_constant<int, 9>());
+      }
+      fence_proxy_async();
+      mbar_arrive(bfull_s + 8 * (p & 1));
+    };
+    build_b(0);
+    for (int p = 0; p < pn; p++) {
+      if (p + 1 < pn) {
+        // the weight buffer of point p + 1 was last read by the MMAs of point p - 1
+        if (p >= 1 && !wait(bempty_s + 8 * ((p + 1) & 1), (unsigned)((((p + 1) >> 1) - 1) & 1))) break;
+        build_b(p + 1);
+      }
+      const int bb = p & 1;
+      if (!wait(tfull_s + 8 * bb, (unsigned)((p >> 1) & 1))) break;
+      tc_fence_after();
+      float o[10][1];
+      const unsigned taddr = tmem + ((unsigned)((warp & 3) * 32) << 16) + bb * kTcN;
+      if constexpr (VGH) {
+        uint32_t r[32];
+        tmem_ld32(taddr, r);
+        tc_fence_before();
+        mbar_arrive(tempty_s + 8 * bb);
+#pragma unroll
+        for (int q = 0; q < 10; q++) o[q][0] = (__uint_as_float(r[2 * q]) + __uint_as_float(r[2 * q + 1])) * sc;
+        // delta_inv factors of the derivatives
+        o[1][0] *= dx; o[2][0] *= dy; o[3][0] *= dz;
+        o[4][0] *= dx * dx; o[5][0] *= dx * dy; o[6][0] *= dx * dz;
+        o[7][0] *= dy * dy; o[8][0] *= dy * dz; o[9][0] *= dz * dz;
+      } else {
+        uint32_t r[2];
+        tmem_ld2(taddr, r);
+        tc_fence_before();
+        mbar_arrive(tempty_s + 8 * bb);
+        o[0][0] = (__uint_as_float(r[0]) + __uint_as_float(r[1])) * sc;
+      }
+      if (col < a.ncol) epilogue<float, 1, VGH, false>(a, ssrc[p], col, o);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (*abort_flag) {
+    // a wait ran out: report it, and let no copy or MMA outlive the block
+    if (tid == 0) {
+      if (a.wait_err) {
+        *(volatile int *)a.wait_err = 1;
+        __threadfence_system();
+      }
+      for (int q = *consumed; q < issued; q++)
+        if (q != skipped) mbar_wait(full_s + 8 * (q % NS), (unsigned)((q / NS) & 1), lim);
+    }
+    if (tid == 32 && last_commit >= 0)
+      mbar_wait(tfull_s + 8 * (last_commit & 1), (unsigned)((last_commit >> 1) & 1), lim);
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
+}
+
 // Index of third-derivative entry m (3x3x3 row-major, m = 9a + 3b + c) among
 // the ten distinct ones (xxx, xxy, xxz, xyy, xyz, xzz, yyy, yyz, yzz, zzz).
 __device__ __forceinline__ int g27to10(int m) {
@@ -667,6 +912,8 @@ static const void *kernel_for(int mode) {
     if constexpr (ST == ST_DF) {
       if (mode == 2 || mode == 3) return (const void *)k_eval_pipe_df<VGH>;
     } else {
+      if constexpr (ST == ST_F16)
+        if (mode == 5) return (const void *)k_eval_tc<VGH>;
       if (mode == 2) return (const void *)k_eval_pipe<ST, VGH, false>;
       if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
     }
@@ -708,21 +955,23 @@ static EncodeTiled encoder() {
 
 // Tensor map of a table's coefficients (base: the stored table or its
 // double-float shadow, es bytes per stored real) as [x][y][z][column], one
-// box = box_cols columns x 4 z x 4 y x 1 x.  Columns past ncol_pad read as
-// zero.  The base is a cudaMalloc address and every stride a multiple of the
-// 128-byte row, so the encoder's 16-byte rules hold.
-static int encode_table_map(const Table *t, const void *base, int es, int box_cols, CUtensorMap *map) {
+// box = box_cols columns x 4 z x 4 y x box_x x (box_x 4 with the 128-byte
+// swizzle: the whole stencil in the tensor cores' operand layout).  Columns
+// past ncol_pad read as zero.  The base is a cudaMalloc address and every
+// stride a multiple of the 128-byte row, so the encoder's 16-byte rules hold.
+static int encode_table_map(const Table *t, const void *base, int es, int box_cols, CUtensorMap *map,
+                            int box_x = 1, CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_NONE) {
   EncodeTiled fn = encoder();
   if (!fn) return fail(EINSPLINE_GB300_ECUDA, "cuTensorMapEncodeTiled is not available");
   const cuuint64_t dims[4] = {(cuuint64_t)t->ncol_pad, (cuuint64_t)t->Nc[2], (cuuint64_t)t->Nc[1],
                               (cuuint64_t)t->Nc[0]};
   const cuuint64_t strides[3] = {(cuuint64_t)(t->zs * es), (cuuint64_t)(t->ys * es), (cuuint64_t)(t->xs * es)};
-  const cuuint32_t box[4] = {(cuuint32_t)box_cols, 4, 4, 1};
+  const cuuint32_t box[4] = {(cuuint32_t)box_cols, 4, 4, (cuuint32_t)box_x};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   const CUtensorMapDataType dt =
       es == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : es == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32 : CU_TENSOR_MAP_DATA_TYPE_UINT64;
   const CUresult r = fn(map, dt, 4, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                        swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(EINSPLINE_GB300_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return 0;
 }
@@ -749,6 +998,9 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   a.mode = mode >= 0 ? mode : pick_mode(t, vgh, a.perm != nullptr);
   const int ks = kernel_storage(t);
   if (a.mode >= 2 && ks == ST_F64) a.mode = 0;        // IEEE FP64 is FMA-bound: no pipeline variant
+  // tensor cores: F16 tables; one column a thread, so not the complex CPU
+  // layout, whose outputs interleave a spline's two columns
+  if (a.mode == 5 && (t->storage != ST_F16 || (a.is_complex && a.layout == 1))) a.mode = is16(t->storage) ? 3 : 2;
   if (a.mode == 3 && !is16(t->storage)) a.mode = 2;   // the wide variant is for 16-bit tables
   const int VW = elems_per_thread(t) * ((a.mode == 3 || (a.mode == 4 && is16(t->storage))) ? 2 : 1);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
@@ -758,7 +1010,14 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
     a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
   }
   if (ks == ST_DF) a.coefs = t->df_coefs;
-  if (a.mode == 4) {
+  if (a.mode == 5) {
+    tx = kTcThreads;
+    ty = 1;
+    a.ntiles = (a.ncol + kTcCols - 1) / kTcCols;
+    a.wait_err = t->wait_err_d;
+    if (int r = encode_table_map(t, a.coefs, 2, 64, &a.tmap, 4, CU_TENSOR_MAP_SWIZZLE_128B)) return r;
+    *smem = tc_smem(pb);
+  } else if (a.mode == 4) {
     ty = 1;
     // narrower tiles where the stage buffers would not fit in shared memory
     const int stages = ks == ST_DF ? TmaStages<ST_DF>::value : kTmaStages;
@@ -842,7 +1101,7 @@ int launch_eval(Table *t, EvalArgs &a, bool vgh, cudaStream_t s, int tx, int ty,
   dim3 block;
   size_t smem;
   if (int r = shape_launch(t, a, vgh, tx, ty, pb, &func, &block, &smem, mode)) return r;
-  if (a.mode == 4 && t->test_skip.load(std::memory_order_relaxed)) {
+  if ((a.mode == 4 || a.mode == 5) && t->test_skip.load(std::memory_order_relaxed)) {
     a.test_skip = t->test_skip.exchange(0);
     a.wait_ns = t->test_wait_ns;
   }

@@ -599,4 +599,71 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
       : "memory");
 }
 
+
+// ------------------------------------------------------------ tensor cores
+// Shared-memory matrix descriptor of a tcgen05.mma operand: start address,
+// leading and stride byte offsets (16-byte units), descriptor version 1 and
+// the swizzle mode (0 none, 2 128-byte).  For an MN-major operand in the
+// 128-byte swizzle the leading offset steps between 64-element atoms along
+// M or N and the stride offset between groups of 8 rows along K; for a
+// K-major operand without swizzle, core matrices are 8 rows of 16 bytes,
+// the leading offset steps along K and the stride offset along M or N.
+__device__ __forceinline__ uint64_t umma_desc(unsigned addr, unsigned lbo, unsigned sbo, unsigned swizzle) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | (uint64_t)((lbo >> 4) & 0x3FFFu) << 16 |
+         (uint64_t)((sbo >> 4) & 0x3FFFu) << 32 | (uint64_t)1 << 46 | (uint64_t)(swizzle & 7u) << 61;
+}
+// Instruction descriptor of a kind::f16 MMA: f16 A and B, f32 accumulator,
+// A MN-major, B K-major, shape M x N.
+__host__ __device__ constexpr uint32_t umma_idesc_f16(int M, int N) {
+  return (1u << 4) | (1u << 15) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+// D[tmem] (+)= A * B for one K = 16 step, issued by one thread.
+__device__ __forceinline__ void umma_f16(unsigned tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"((unsigned)acc)
+      : "memory");
+}
+// Arrives once on mbarrier bar when every MMA this thread issued so far is complete.
+__device__ __forceinline__ void umma_commit(unsigned bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// Orders this thread's generic shared-memory writes before later reads of
+// the same memory by the async proxy (tensor cores, bulk copies).
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// 32 consecutive accumulator columns of this thread's TMEM lane (the warp
+// reads lanes 32 * (warp % 4) .. + 31).
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld2(unsigned taddr, uint32_t (&r)[2]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Tensor-core evaluation (load mode 5) shared memory: the points' weights,
+// cells and sources; slack to align the operand area to 1024 bytes (the
+// 128-byte swizzle atom); kTcStages stencil buffers of 64 rows x 128 f16
+// columns (16 KB, two 8 KB boxes of 64 columns); two 4 KB weight matrices
+// (64 x 32 f16); mbarriers (two per stage, two per weight buffer and per
+// accumulator); the TMEM address, an abort flag and a count.
+constexpr int kTcStages = 3;
+constexpr int kTcCols = 128;    // columns per block (the MMA's M)
+constexpr int kTcN = 32;        // 10 outputs x (hi, lo) weights, padded to 32
+constexpr int kTcThreads = 192; // copy warp, MMA warp, 4 weight/output warps
+__host__ __device__ __forceinline__ size_t tc_smem(int pb) {
+  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
+}
+
 }  // namespace eg

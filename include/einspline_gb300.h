@@ -186,21 +186,30 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  *      one copy brings the 4x4 stencil rows of a point's x-plane for the
  *      whole block, completion is tracked by mbarriers; 8 columns a thread
  *      for 16-bit tables, 4 for FP32, 2 for double-float (IEEE FP64 uses 0);
+ *   5: F16 tables: the reduction runs on the tensor cores (tcgen05.mma):
+ *      a block of 128 threads owns 128 columns, one TMA copy per 64 columns
+ *      brings a point's whole 4x4x4 stencil in the MMA operand layout, and
+ *      the point's weights, split into f16 high and low parts, are the other
+ *      operand; FP32 accumulation in tensor memory.  Results agree with the
+ *      other modes to FP32 rounding, not bit for bit, so the autotuner never
+ *      picks it.  Other tables, and complex tables in the CPU layout, use
+ *      their pipeline (3 or 2) instead;
  *  -1: the autotuned choice; untuned, vgh uses 3 for 16-bit tables and 2
  *      for FP32 (the choices the autotuner makes on GB300), value-only and
- *      FP64 use 0.  Results are identical in all modes. */
+ *      FP64 use 0.  Results are identical in modes 0-4. */
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode);
 int einspline_gb300_get_load_mode(einspline_gb300_table *t);
-/* Every wait of the mode-4 kernels on their mbarriers is bounded (0.5 s);
+/* Every wait of the mode-4 and mode-5 kernels on their mbarriers is bounded (0.5 s);
  * one that runs out makes the block stop early and sets a word that this
  * call reads and clears: EINSPLINE_GB300_ETIMEOUT when some launch on t since
  * the last check gave up (its results are incomplete), else 0.  Call it
  * after the launches have completed (synchronised stream).  The blocking
  * entries (single-point, host-buffer) check it themselves. */
 int einspline_gb300_wait_status(einspline_gb300_table *t);
-/* Testing the bounded waits without a fault: the next mode-4 launch on t
- * has its first block issue no copy for its stage `stage` (stages count a
- * block's point x-planes from 0), and every wait of that launch gives up
+/* Testing the bounded waits without a fault: the next mode-4 or mode-5 launch
+ * on t has its first block issue no copy for its stage `stage` (stages count
+ * a block's point x-planes from 0 in mode 4, its points in mode 5), and every
+ * wait of that launch gives up
  * after `seconds` (1 us .. 1 s) instead of 0.5 s.  That stage's barrier
  * then never completes, its wait runs out, the block stops early and the
  * launch reports ETIMEOUT through einspline_gb300_wait_status; no copy is

@@ -148,7 +148,7 @@ def test_tma_mode_arguments():
     G.set_load_mode(4)
     assert G.get_load_mode() == 4
     with pytest.raises(api.EinsplineError):
-        G.set_load_mode(5)
+        G.set_load_mode(6)
     G.wait_status()
 
 
