@@ -38,7 +38,9 @@ UNIT = "spline-evals/s"
 BYTES_F32 = 64 * 4 + 10 * 4   # algorithmic bytes per vgh spline-eval, FP32 table
 BYTES_F16 = 64 * 2 + 10 * 4   # FP16 table (per-spline scale amortised to 0)
 KERNEL_BY_MODE = {0: "k_eval<F16,vgh>", 1: "k_eval<F16,vgh> (L2 bulk prefetch)", 2: "k_eval_pipe<F16,vgh>",
-                  3: "k_eval_pipe<F16,vgh,wide>"}
+                  3: "k_eval_pipe<F16,vgh,wide>", 4: "k_eval_tma<F16,vgh>", 5: "k_eval_tc<vgh> (tensor cores)"}
+# DRAM bytes per eval measured by ncu for the kernel of each load mode (profiles/traffic.json)
+TRAFFIC_KEY_BY_MODE = {3: "f16_vgh_bytes_per_eval", 5: "f16_vgh_tc_bytes_per_eval"}
 
 
 def dist_env():
@@ -492,7 +494,8 @@ def run_gpu(args):
     evals_per_launch = ev16 / args.steps / world
     peak, peak_kind = measured_peak()
     achieved = evals_per_launch * BYTES_F16 / (per_launch_ms / 1e3) / 1e9
-    tr = profile_traffic("f16_vgh_bytes_per_eval")
+    tr_key = TRAFFIC_KEY_BY_MODE.get(tiles["f16"]["load_mode"])
+    tr = profile_traffic(tr_key) if tr_key else None
 
     # end to end through the host-buffer C-ABI entry: pinned positions in,
     # pinned results out, copies inside the timed region

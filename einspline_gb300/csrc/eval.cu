@@ -520,34 +520,35 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
 
 // Tensor-core evaluation (load mode 5, F16 tables).  For one point the ten
 // outputs of a column are a product of the point's 10 x 64 stencil weights
-// with the column's 64 stencil coefficients, so a block owns 128
-// consecutive columns and, point after point of its group, computes
-//   D[128 columns x 32] = A[128 columns x 64 rows] * B[64 rows x 32]
-// with four tcgen05.mma (M 128, N 32, K 16: one per x-plane) into an f32
-// accumulator in tensor memory.  A is the stencil exactly as stored: two TMA
-// boxes of 64 columns x 4 z x 4 y x 4 x, in the 128-byte swizzle, which is
-// the MN-major operand layout.  B holds each output's weights w_x w_y w_z
-// (computed in FP32 without the delta_inv factors) split into f16 high and
-// low parts, one column each: output q = D[2q] + D[2q+1], then times its
-// delta_inv factors, the spline's factor and the point's sign.  The
-// products of f16 coefficients with the 22-bit weights are exact and the
-// sums are FP32, so results agree with the FMA kernels to FP32 rounding
-// (not bit for bit).
+// with the column's 64 stencil coefficients, so for each 128-column tile of
+// its kTcCols columns a block computes, point after point of its group,
+//   D[128 columns x 16] = A[128 columns x 64 rows] * B[64 rows x 16]
+// with tcgen05.mma (M 128, N 16, K 16) into an f32 accumulator in tensor
+// memory.  A is the stencil exactly as stored: TMA boxes of 64 columns x 4 z
+// x 4 y x 4 x in the 128-byte swizzle, which is the MN-major operand
+// layout.  B holds each output's weight w_x w_y w_z (FP32, without the
+// delta_inv factors) split into f16 high and low parts: eight K steps per
+// tile, the four x-planes against the high parts and again against the low
+// parts, so each output accumulates the exact products of its 22-bit weight
+// in one FP32 column; it is then scaled by its delta_inv factors, the
+// spline's factor and the point's sign.  Results agree with the FMA kernels
+// to FP32 rounding (not bit for bit).
 // Warp roles, synchronised only through mbarriers: warp 0 (one lane) keeps
 // the stencil copies of up to kTcStages points in flight; warp 1 (one lane)
 // issues each point's MMAs once its stencil, its weight matrix and a free
 // accumulator are there, and commits them to the barriers that free the
-// stage, the weight buffer and fill the accumulator; warps 2-5 (one column a
-// thread, each warp the TMEM lanes of its quarter) build the next point's
-// weight matrix, then read this point's accumulator and store its outputs.
-// Weight matrices and accumulators are double-buffered.  Every wait is
-// bounded and also ends when another role gave up (a shared flag): a block
-// that gave up sets a.wait_err, waits (again bounded) for its copies and
-// MMAs in flight, and frees its tensor memory.
+// stage, free the weight buffer and fill the accumulator; warps 2-5 (each
+// the TMEM lanes of its quarter: one column of every tile a thread) build
+// the next point's weight matrix, then read this point's accumulator and
+// store its outputs.  Weight matrices and accumulators are double-buffered.
+// Every wait is bounded and also ends once another role gave up (a shared
+// flag): a block that gave up sets a.wait_err, waits (again bounded) for its
+// copies and MMAs in flight, and frees its tensor memory.
 template <bool VGH>
 __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr int NS = kTcStages;
+  constexpr int NS = kTcStages, T = kTcTiles;
+  constexpr unsigned kStage = T * 16384u, kAcc = T * kTcN;  // stage bytes, TMEM columns per accumulator
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tile = blockIdx.x % a.ntiles;
   const int64_t grp = blockIdx.x / a.ntiles;
@@ -573,7 +574,7 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
   }
   const unsigned base_s = (unsigned)__cvta_generic_to_shared(smem);
   const unsigned a_s = (base_s + (unsigned)smem_total(a.pb, 4) + 1023u) & ~1023u;
-  const unsigned b_s = a_s + NS * 16384u;
+  const unsigned b_s = a_s + NS * kStage;
   // mbarriers: full/empty per stage; weight matrix full/empty, accumulator
   // full/empty per buffer; then the TMEM address, the abort flag and the
   // count of points whose stencil the MMA warp consumed
@@ -582,10 +583,11 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
   unsigned char *bgen = smem + (b_s - base_s);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + (slot_s + 4 - base_s));
   volatile int *consumed = reinterpret_cast<volatile int *>(smem + (slot_s + 8 - base_s));
-  // weight columns 20..31 (and all but 0, 1 for value only) stay zero
+  // weight columns 10..15 (and all but 0 for value only) stay zero
   for (int e = tid; e < 2 * 4096 / 16; e += kTcThreads) reinterpret_cast<uint4 *>(bgen)[e] = make_uint4(0, 0, 0, 0);
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(slot_s) : "memory");
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_s), "n"(2 * kAcc)
+                 : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 32) {
@@ -596,10 +598,10 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
     }
 #pragma unroll
     for (int b = 0; b < 2; b++) {
-      mbar_init(bfull_s + 8 * b, kTcCols);
+      mbar_init(bfull_s + 8 * b, 128);
       mbar_init(bempty_s + 8 * b, 1);
       mbar_init(tfull_s + 8 * b, 1);
-      mbar_init(tempty_s + 8 * b, kTcCols);
+      mbar_init(tempty_s + 8 * b, 128);
     }
     *abort_flag = 0;
     *consumed = 0;
@@ -630,17 +632,17 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
         issued = p + 1;
         // test hook: no copy for this point, so its wait runs out
         if (a.test_skip == p + 1 && blockIdx.x == 0) { skipped = p; continue; }
-        mbar_arrive_expect_tx(full_s + 8 * s, 16384u);
+        mbar_arrive_expect_tx(full_s + 8 * s, kStage);
 #pragma unroll
-        for (int mg = 0; mg < 2; mg++)
-          tma_load_4d(a_s + s * 16384u + mg * 8192u, &a.tmap, full_s + 8 * s, c_first + 64 * mg, sidx[3 * p + 2],
+        for (int mg = 0; mg < 2 * T; mg++)
+          tma_load_4d(a_s + s * kStage + mg * 8192u, &a.tmap, full_s + 8 * s, c_first + 64 * mg, sidx[3 * p + 2],
                       sidx[3 * p + 1], sidx[3 * p]);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMAs
-      constexpr uint32_t idesc = umma_idesc_f16(kTcCols, kTcN);
+      // MMAs: per tile, the four x-planes against the high, then the low weights
+      constexpr uint32_t idesc = umma_idesc_f16(128, kTcN);
       for (int p = 0; p < pn; p++) {
         const int s = p % NS, bb = p & 1;
         if (!wait(full_s + 8 * s, (unsigned)((p / NS) & 1))) break;
@@ -649,9 +651,14 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
         if (p >= 2 && !wait(tempty_s + 8 * bb, (unsigned)(((p >> 1) - 1) & 1))) break;
         tc_fence_after();
 #pragma unroll
-        for (int i = 0; i < 4; i++)
-          umma_f16(tmem + bb * kTcN, umma_desc(a_s + s * 16384u + i * 2048u, 8192u, 1024u, 2),
-                   umma_desc(b_s + bb * 4096u + i * 1024u, 128u, 256u, 0), idesc, i > 0);
+        for (int t = 0; t < T; t++)
+#pragma unroll
+          for (int h = 0; h < 2; h++)
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+              umma_f16(tmem + bb * kAcc + t * kTcN,
+                       umma_desc(a_s + s * kStage + t * 16384u + i * 2048u, 8192u, 1024u, 2),
+                       umma_desc(b_s + bb * 4096u + (h * 4 + i) * 512u, 128u, 256u, 0), idesc, h > 0 || i > 0);
         umma_commit(empty_s + 8 * s);
         umma_commit(bempty_s + 8 * bb);
         umma_commit(tfull_s + 8 * bb);
@@ -659,33 +666,43 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
       }
     }
   } else {
-    // weight matrices and outputs: thread et owns column c_first + colr
+    // weight matrices and outputs: thread et owns column colr of every tile
     const int et = tid - 64;
     const int colr = (warp & 3) * 32 + lane;
-    const int col = c_first + colr;
     // this thread's share of a weight matrix: stencil row k, outputs 0-4
     // (even threads) or 5-9 (odd threads)
     const int k = et >> 1;
     const int ki = k >> 4, kj = (k >> 2) & 3, km = k & 3, kk = k & 15;
-    const unsigned boff = ki * 1024 + (kk >> 3) * 128 + (kk & 7) * 2;
+    const unsigned boff = ki * 512 + (kk >> 3) * 128 + (kk & 7) * 2;
     // derivative orders in x, y, z of each output (v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz)
     static constexpr int OA[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
     static constexpr int OB[10] = {0, 0, 1, 0, 0, 1, 0, 2, 1, 0};
     static constexpr int OC[10] = {0, 0, 0, 1, 0, 0, 1, 0, 1, 2};
-    const float dx = a.dinvf[0], dy = a.dinvf[1], dz = a.dinvf[2];
-    const float sc = (a.scale && col < a.ncol) ? a.scale[col] : 1.f;
+    // per column: the spline's factor times each output's delta_inv factors
+    float f[T][10];
+    {
+      const float dx = a.dinvf[0], dy = a.dinvf[1], dz = a.dinvf[2];
+      const float d[10] = {1.f, dx, dy, dz, dx * dx, dx * dy, dx * dz, dy * dy, dy * dz, dz * dz};
+#pragma unroll
+      for (int t = 0; t < T; t++) {
+        const int col = c_first + t * 128 + colr;
+        const float sc = (a.scale && col < a.ncol) ? a.scale[col] : 1.f;
+#pragma unroll
+        for (int q = 0; q < 10; q++) f[t][q] = sc * d[q];
+      }
+    }
     // Weight matrix of point p into buffer p & 1, then arrive on its barrier.
     auto build_b = [&](int p) {
       const float *w = sw + p * 36;
       unsigned char *bm = bgen + (p & 1) * 4096 + boff;
-      // weight of output q at this row, as f16 high and low parts in columns 2q, 2q + 1
+      // weight of output q at this row: f16 high part in the high tiles, low part in the low tiles
       auto put = [&](auto qc) {
         constexpr int q = decltype(qc)::value;
         const float wq = w[OA[q] * 4 + ki] * w[12 + OB[q] * 4 + kj] * w[24 + OC[q] * 4 + km];
         const __half hi = __float2half_rn(wq);
         const __half lo = __float2half_rn(wq - __half2float(hi));
-        *reinterpret_cast<__half *>(bm + ((2 * q) >> 3) * 256 + ((2 * q) & 7) * 16) = hi;
-        *reinterpret_cast<__half *>(bm + ((2 * q + 1) >> 3) * 256 + ((2 * q + 1) & 7) * 16) = lo;
+        *reinterpret_cast<__half *>(bm + (q >> 3) * 256 + (q & 7) * 16) = hi;
+        *reinterpret_cast<__half *>(bm + 2048 + (q >> 3) * 256 + (q & 7) * 16) = lo;
       };
       if (!(et & 1)) {
         put(std::integral_constant<int, 0>());
@@ -715,27 +732,22 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
       const int bb = p & 1;
       if (!wait(tfull_s + 8 * bb, (unsigned)((p >> 1) & 1))) break;
       tc_fence_after();
-      float o[10][1];
-      const unsigned taddr = tmem + ((unsigned)((warp & 3) * 32) << 16) + bb * kTcN;
-      if constexpr (VGH) {
-        uint32_t r[32];
-        tmem_ld32(taddr, r);
-        tc_fence_before();
-        mbar_arrive(tempty_s + 8 * bb);
+      uint32_t r[32];
+      static_assert(T * kTcN <= 32, "one load reads every tile's accumulator");
+      if constexpr (T * kTcN == 32) tmem_ld32(tmem + ((unsigned)((warp & 3) * 32) << 16) + bb * kAcc, r);
+      else tmem_ld16(tmem + ((unsigned)((warp & 3) * 32) << 16) + bb * kAcc, r);
+      tc_fence_before();
+      mbar_arrive(tempty_s + 8 * bb);
+      const int64_t src = ssrc[p];
 #pragma unroll
-        for (int q = 0; q < 10; q++) o[q][0] = (__uint_as_float(r[2 * q]) + __uint_as_float(r[2 * q + 1])) * sc;
-        // delta_inv factors of the derivatives
-        o[1][0] *= dx; o[2][0] *= dy; o[3][0] *= dz;
-        o[4][0] *= dx * dx; o[5][0] *= dx * dy; o[6][0] *= dx * dz;
-        o[7][0] *= dy * dy; o[8][0] *= dy * dz; o[9][0] *= dz * dz;
-      } else {
-        uint32_t r[2];
-        tmem_ld2(taddr, r);
-        tc_fence_before();
-        mbar_arrive(tempty_s + 8 * bb);
-        o[0][0] = (__uint_as_float(r[0]) + __uint_as_float(r[1])) * sc;
+      for (int t = 0; t < T; t++) {
+        const int col = c_first + t * 128 + colr;
+        if (col >= a.ncol) continue;
+        float o[10][1];
+#pragma unroll
+        for (int q = 0; q < (VGH ? 10 : 1); q++) o[q][0] = __uint_as_float(r[t * kTcN + q]) * f[t][q];
+        epilogue<float, 1, VGH, false>(a, src, col, o);
       }
-      if (col < a.ncol) epilogue<float, 1, VGH, false>(a, ssrc[p], col, o);
     }
   }
   tc_fence_before();
@@ -755,7 +767,7 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
   }
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(2 * kAcc) : "memory");
 }
 
 // Index of third-derivative entry m (3x3x3 row-major, m = 9a + 3b + c) among
@@ -1163,6 +1175,11 @@ int pick_mode(Table *t, bool vgh, bool sorted) {
   const int v = vgh ? 1 : 0;
   if (sorted && t->tuned_s_tx[v]) return t->tuned_s_mode[v];
   if (t->tuned_tx[v]) return t->tuned_mode[v];
+  // F16 vgh: the tensor-core reduction (64^3 x 1024, 64 walkers: 45.0 G
+  // evals/s random and 54.1 G cell-sorted against 43.0 G and 44.6 G for the
+  // wide copy pipeline); value only stays on the wide pipeline (58.4 G
+  // random and 90.9 G sorted against 57.8 G and 74.0 G)
+  if (vgh && t->storage == ST_F16) return 5;
   if (vgh && kernel_storage(t) != ST_F64) return is16(t->storage) ? 3 : 2;
   // value only: the wide pipeline for 16-bit tables (0.294 against 0.413 ms
   // with direct loads at 64^3 x 1024, 17k points); FP32 is as fast direct
@@ -1175,6 +1192,14 @@ void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb, bool
   const int v = vgh ? 1 : 0;
   if (sorted && t->tuned_s_tx[v]) { tx = t->tuned_s_tx[v]; ty = t->tuned_s_ty[v]; pb = t->tuned_s_pb[v]; return; }
   if (t->tuned_tx[v]) { tx = t->tuned_tx[v]; ty = t->tuned_ty[v]; pb = t->tuned_pb[v]; return; }
+  if (t->storage == ST_F16 && ((vgh && t->tile_mode < 0) || t->tile_mode == 5)) {
+    // tensor cores: 10 points a block keep three blocks on an SM (74.7 KB of
+    // shared memory each); the block's threads are fixed by the kernel
+    tx = 128;
+    ty = 1;
+    pb = 10;
+    return;
+  }
   const int VW = elems_per_thread(t);
   const int need = (t->ncol + VW - 1) / VW;
   tx = (need + 31) / 32 * 32;

@@ -647,23 +647,34 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, uint32_t (&r)[32]) {
       : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
 __device__ __forceinline__ void tmem_ld2(unsigned taddr, uint32_t (&r)[2]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Tensor-core evaluation (load mode 5) shared memory: the points' weights,
+// Tensor-core evaluation (load mode 5).  A block owns kTcTiles tiles of 128
+// columns (each the M of one MMA).  Shared memory: the points' weights,
 // cells and sources; slack to align the operand area to 1024 bytes (the
-// 128-byte swizzle atom); kTcStages stencil buffers of 64 rows x 128 f16
-// columns (16 KB, two 8 KB boxes of 64 columns); two 4 KB weight matrices
-// (64 x 32 f16); mbarriers (two per stage, two per weight buffer and per
-// accumulator); the TMEM address, an abort flag and a count.
-constexpr int kTcStages = 3;
-constexpr int kTcCols = 128;    // columns per block (the MMA's M)
-constexpr int kTcN = 32;        // 10 outputs x (hi, lo) weights, padded to 32
-constexpr int kTcThreads = 192; // copy warp, MMA warp, 4 weight/output warps
+// 128-byte swizzle atom); kTcStages stencil buffers of 64 rows x kTcCols f16
+// columns (16 KB a tile, as 8 KB boxes of 64 columns); two weight buffers of
+// eight 16 x 16 K-major tiles (the f16 high parts of the four x-planes, then
+// the low parts: 4 KB); mbarriers (two per stage, two per weight buffer and
+// per accumulator); the TMEM address, an abort flag and a count.
+constexpr int kTcStages = 2;
+constexpr int kTcTiles = 2;
+constexpr int kTcCols = 128 * kTcTiles;  // columns per block
+constexpr int kTcN = 16;                 // 10 outputs, padded to the MMA's N
+constexpr int kTcThreads = 192;          // copy warp, MMA warp, 4 weight/output warps
 __host__ __device__ __forceinline__ size_t tc_smem(int pb) {
-  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
+  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * kTcTiles * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
 }
 
 }  // namespace eg

@@ -191,12 +191,14 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  *      brings a point's whole 4x4x4 stencil in the MMA operand layout, and
  *      the point's weights, split into f16 high and low parts, are the other
  *      operand; FP32 accumulation in tensor memory.  Results agree with the
- *      other modes to FP32 rounding, not bit for bit, so the autotuner never
- *      picks it.  Other tables, and complex tables in the CPU layout, use
- *      their pipeline (3 or 2) instead;
- *  -1: the autotuned choice; untuned, vgh uses 3 for 16-bit tables and 2
- *      for FP32 (the choices the autotuner makes on GB300), value-only and
- *      FP64 use 0.  Results are identical in modes 0-4. */
+ *      other modes to FP32 rounding, not bit for bit.  It is the default of
+ *      vgh on F16 tables, whose vgh autotuning only tunes its points per
+ *      block, so tuning changes no result.  Other tables, and complex tables
+ *      in the CPU layout, use their pipeline (3 or 2) instead;
+ *  -1: the autotuned choice; untuned, vgh uses 5 for F16 tables, 3 for the
+ *      other 16-bit tables and 2 for FP32 (the choices the autotuner makes
+ *      on GB300); value-only uses 3 for 16-bit tables and 0 for FP32; FP64
+ *      uses 0.  Results are identical in modes 0-4, and within mode 5. */
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode);
 int einspline_gb300_get_load_mode(einspline_gb300_table *t);
 /* Every wait of the mode-4 and mode-5 kernels on their mbarriers is bounded (0.5 s);
@@ -328,7 +330,9 @@ typedef struct {
  *   row_d[w][j]   = phi_j(r_w), j < N                           (optional)
  * with r_w = pos_d[3w..3w+2].  The orbital values, gradients and Laplacians
  * are never written to memory (except the value row when row_d != NULL); the
- * row equals einspline_gb300_eval_3d's values bit for bit.  Sums run in a
+ * row equals einspline_gb300_eval_3d's values bit for bit in load modes 0-4
+ * (the FMA reduction; F16 tables default to the tensor-core mode 5, which
+ * agrees with it to FP32 rounding).  Sums run in a
  * fixed order, so results do not vary from run to run.  Asynchronous on
  * stream (NULL = legacy default stream). */
 int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_det_opts *opts, int nwalkers,

@@ -38,7 +38,9 @@ def _population(torch, orc, G, T, W, seed, trans, nelec=NELEC, ld=LD, distinct=N
 
 def _check_ratio(orc, torch, G, D, Ai, pos, k, trans, nelec):
     """Ratios of the fused kernel against float64 sums of the flat
-    evaluation's per-orbital outputs, the value row bit for bit."""
+    evaluation's per-orbital outputs, the value row bit for bit with the
+    flat evaluation's FMA reduction (load modes 0-4: F16 tables otherwise
+    default to the tensor-core mode)."""
     W, ld = Ai.shape[0], Ai.shape[1]
     rows = torch.zeros(W, ld, dtype=torch.float32, device="cuda")
     r, g, lap = D.ratio(G, pos, k, grad_lapl=True, rows=rows)
@@ -47,7 +49,9 @@ def _check_ratio(orc, torch, G, D, Ai, pos, k, trans, nelec):
     torch.cuda.synchronize()
     assert torch.equal(r, r2) and torch.equal(g, g2) and torch.equal(lap, l2)
     assert g0 is None and l0 is None
+    G.set_load_mode(2)
     v, gr, h = G.eval(pos, vgh=True, rule=1, layout=1)
+    G.set_load_mode(-1)
     assert torch.equal(rows[:, :nelec], v[:, :nelec])
     assert torch.count_nonzero(rows[:, nelec:]) == 0
     Astd = _ainv_std(Ai, trans)[:, :nelec, :nelec]
