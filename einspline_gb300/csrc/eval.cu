@@ -678,6 +678,8 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
     static constexpr int OA[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
     static constexpr int OB[10] = {0, 0, 1, 0, 0, 1, 0, 2, 1, 0};
     static constexpr int OC[10] = {0, 0, 0, 1, 0, 0, 1, 0, 1, 2};
+    // the common batched form: flat outputs in the GPU layout, no sign
+    const bool plain = VGH && a.out == 0 && a.layout == 0 && !a.vals_pp && !a.grads_pp && !a.hess_pp && !a.sign;
     // per column: the spline's factor times each output's delta_inv factors
     float f[T][10];
     {
@@ -695,10 +697,18 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
     auto build_b = [&](int p) {
       const float *w = sw + p * 36;
       unsigned char *bm = bgen + (p & 1) * 4096 + boff;
+      // the nine basis weights of this stencil row (value, d1, d2 per axis)
+      float wx[3], wy[3], wz[3];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        wx[d] = w[4 * d + ki];
+        wy[d] = w[12 + 4 * d + kj];
+        wz[d] = w[24 + 4 * d + km];
+      }
       // weight of output q at this row: f16 high part in the high tiles, low part in the low tiles
       auto put = [&](auto qc) {
         constexpr int q = decltype(qc)::value;
-        const float wq = w[OA[q] * 4 + ki] * w[12 + OB[q] * 4 + kj] * w[24 + OC[q] * 4 + km];
+        const float wq = wx[OA[q]] * wy[OB[q]] * wz[OC[q]];
         const __half hi = __float2half_rn(wq);
         const __half lo = __float2half_rn(wq - __half2float(hi));
         *reinterpret_cast<__half *>(bm + (q >> 3) * 256 + (q & 7) * 16) = hi;
@@ -739,6 +749,26 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
       tc_fence_before();
       mbar_arrive(tempty_s + 8 * bb);
       const int64_t src = ssrc[p];
+      if (plain) {
+        // flat GPU layout: value, 3 gradient and 6 Hessian reals per column
+        float *vp = reinterpret_cast<float *>(a.vals) + src * a.vstride;
+        float *gp = reinterpret_cast<float *>(a.grads) + src * a.gstride;
+        float *hp = reinterpret_cast<float *>(a.hess) + src * a.hstride;
+#pragma unroll
+        for (int t = 0; t < T; t++) {
+          const int col = c_first + t * 128 + colr;
+          if (col >= a.ncol) continue;
+          float o[10];
+#pragma unroll
+          for (int q = 0; q < 10; q++) o[q] = __uint_as_float(r[t * kTcN + q]) * f[t][q];
+          vp[col] = o[0];
+#pragma unroll
+          for (int c = 0; c < 3; c++) gp[3 * col + c] = o[1 + c];
+#pragma unroll
+          for (int c = 0; c < 6; c++) hp[6 * col + c] = o[4 + c];
+        }
+        continue;
+      }
 #pragma unroll
       for (int t = 0; t < T; t++) {
         const int col = c_first + t * 128 + colr;
