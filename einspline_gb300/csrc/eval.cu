@@ -548,7 +548,7 @@ template <bool VGH>
 __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NS = kTcStages, T = kTcTiles;
-  constexpr unsigned kStage = T * 16384u, kAcc = T * kTcN;  // stage bytes, TMEM columns per accumulator
+  constexpr unsigned kStage = 16384u, kAcc = T * kTcN;  // bytes of a stage (one tile), TMEM columns per accumulator
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tile = blockIdx.x % a.ntiles;
   const int64_t grp = blockIdx.x / a.ntiles;
@@ -624,45 +624,48 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
   int issued = 0, skipped = -1, last_commit = -1;
   if (warp == 0) {
     if (lane == 0) {
-      // stencil copies
+      // stencil copies, one stage per tile of a point (unit u = p * T + t)
       tma_prefetch_map(&a.tmap);
-      for (int p = 0; p < pn; p++) {
-        const int s = p % NS;
-        if (p >= NS && !wait(empty_s + 8 * s, (unsigned)((p / NS - 1) & 1))) break;
-        issued = p + 1;
+      for (int u = 0; u < pn * T; u++) {
+        const int s = u % NS, p = u / T, t = u % T;
+        if (u >= NS && !wait(empty_s + 8 * s, (unsigned)((u / NS - 1) & 1))) break;
+        issued = u + 1;
         // test hook: no copy for this point, so its wait runs out
         if (a.test_skip == p + 1 && blockIdx.x == 0) { skipped = p; continue; }
         mbar_arrive_expect_tx(full_s + 8 * s, kStage);
 #pragma unroll
-        for (int mg = 0; mg < 2 * T; mg++)
-          tma_load_4d(a_s + s * kStage + mg * 8192u, &a.tmap, full_s + 8 * s, c_first + 64 * mg, sidx[3 * p + 2],
-                      sidx[3 * p + 1], sidx[3 * p]);
+        for (int mg = 0; mg < 2; mg++)
+          tma_load_4d(a_s + s * kStage + mg * 8192u, &a.tmap, full_s + 8 * s, c_first + 128 * t + 64 * mg,
+                      sidx[3 * p + 2], sidx[3 * p + 1], sidx[3 * p]);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       // MMAs: per tile, the four x-planes against the high, then the low weights
       constexpr uint32_t idesc = umma_idesc_f16(128, kTcN);
-      for (int p = 0; p < pn; p++) {
-        const int s = p % NS, bb = p & 1;
-        if (!wait(full_s + 8 * s, (unsigned)((p / NS) & 1))) break;
-        *consumed = p + 1;
+      bool go = true;
+      for (int p = 0; p < pn && go; p++) {
+        const int bb = p & 1;
         if (!wait(bfull_s + 8 * bb, (unsigned)((p >> 1) & 1))) break;
         if (p >= 2 && !wait(tempty_s + 8 * bb, (unsigned)(((p >> 1) - 1) & 1))) break;
-        tc_fence_after();
 #pragma unroll
-        for (int t = 0; t < T; t++)
+        for (int t = 0; t < T; t++) {
+          const int u = p * T + t, s = u % NS;
+          if (!wait(full_s + 8 * s, (unsigned)((u / NS) & 1))) { go = false; break; }
+          *consumed = u + 1;
+          tc_fence_after();
 #pragma unroll
           for (int h = 0; h < 2; h++)
 #pragma unroll
             for (int i = 0; i < 4; i++)
-              umma_f16(tmem + bb * kAcc + t * kTcN,
-                       umma_desc(a_s + s * kStage + t * 16384u + i * 2048u, 8192u, 1024u, 2),
+              umma_f16(tmem + bb * kAcc + t * kTcN, umma_desc(a_s + s * kStage + i * 2048u, 8192u, 1024u, 2),
                        umma_desc(b_s + bb * 4096u + (h * 4 + i) * 512u, 128u, 256u, 0), idesc, h > 0 || i > 0);
-        umma_commit(empty_s + 8 * s);
+          umma_commit(empty_s + 8 * s);
+          last_commit = p;
+        }
+        if (!go) break;
         umma_commit(bempty_s + 8 * bb);
         umma_commit(tfull_s + 8 * bb);
-        last_commit = p;
       }
     }
   } else {
@@ -789,11 +792,14 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
         *(volatile int *)a.wait_err = 1;
         __threadfence_system();
       }
-      for (int q = *consumed; q < issued; q++)
-        if (q != skipped) mbar_wait(full_s + 8 * (q % NS), (unsigned)((q / NS) & 1), lim);
+      for (int u = *consumed; u < issued; u++)
+        if (u / T != skipped) mbar_wait(full_s + 8 * (u % NS), (unsigned)((u / NS) & 1), lim);
     }
-    if (tid == 32 && last_commit >= 0)
-      mbar_wait(tfull_s + 8 * (last_commit & 1), (unsigned)((last_commit >> 1) & 1), lim);
+    // the last MMAs committed complete before their tensor memory is freed
+    if (tid == 32 && last_commit >= 0) {
+      const int u = *consumed - 1;
+      mbar_wait(empty_s + 8 * (u % NS), (unsigned)((u / NS) & 1), lim);
+    }
   }
   __syncthreads();
   tc_fence_after();

@@ -668,13 +668,13 @@ __device__ __forceinline__ void tmem_ld2(unsigned taddr, uint32_t (&r)[2]) {
 // eight 16 x 16 K-major tiles (the f16 high parts of the four x-planes, then
 // the low parts: 4 KB); mbarriers (two per stage, two per weight buffer and
 // per accumulator); the TMEM address, an abort flag and a count.
-constexpr int kTcStages = 2;
+constexpr int kTcStages = 4;  // stencil stages, one 128-column tile of a point each
 constexpr int kTcTiles = 2;
 constexpr int kTcCols = 128 * kTcTiles;  // columns per block
 constexpr int kTcN = 16;                 // 10 outputs, padded to the MMA's N
 constexpr int kTcThreads = 192;          // copy warp, MMA warp, 4 weight/output warps
 __host__ __device__ __forceinline__ size_t tc_smem(int pb) {
-  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * kTcTiles * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
+  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
 }
 
 }  // namespace eg
