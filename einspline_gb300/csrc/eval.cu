@@ -534,10 +534,11 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
 // spline's factor and the point's sign.  Results agree with the FMA kernels
 // to FP32 rounding (not bit for bit).
 // Warp roles, synchronised only through mbarriers: warp 0 (one lane) keeps
-// the stencil copies of up to kTcStages points in flight; warp 1 (one lane)
-// issues each point's MMAs once its stencil, its weight matrix and a free
-// accumulator are there, and commits them to the barriers that free the
-// stage, free the weight buffer and fill the accumulator; warps 2-5 (each
+// up to kTcStages stencil copies in flight, one stage per tile of a point;
+// warp 1 (one lane) issues a tile's MMAs once its stencil, the point's
+// weight matrix and a free accumulator are there, commits each tile to the
+// barrier that frees its stage and each point to those that free the weight
+// buffer and fill the accumulator; warps 2-5 (each
 // the TMEM lanes of its quarter: one column of every tile a thread) build
 // the next point's weight matrix, then read this point's accumulator and
 // store its outputs.  Weight matrices and accumulators are double-buffered.

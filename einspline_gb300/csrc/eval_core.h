@@ -663,8 +663,8 @@ __device__ __forceinline__ void tmem_ld2(unsigned taddr, uint32_t (&r)[2]) {
 // Tensor-core evaluation (load mode 5).  A block owns kTcTiles tiles of 128
 // columns (each the M of one MMA).  Shared memory: the points' weights,
 // cells and sources; slack to align the operand area to 1024 bytes (the
-// 128-byte swizzle atom); kTcStages stencil buffers of 64 rows x kTcCols f16
-// columns (16 KB a tile, as 8 KB boxes of 64 columns); two weight buffers of
+// 128-byte swizzle atom); kTcStages stencil buffers, each 64 rows x 128 f16
+// columns of one tile (16 KB, two 8 KB boxes of 64 columns); two weight buffers of
 // eight 16 x 16 K-major tiles (the f16 high parts of the four x-planes, then
 // the low parts: 4 KB); mbarriers (two per stage, two per weight buffer and
 // per accumulator); the TMEM address, an abort flag and a count.
