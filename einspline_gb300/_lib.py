@@ -199,6 +199,9 @@ def _signatures():
     sig["einspline_gb300_flush"] = ([vp], i32)
     sig["einspline_gb300_get_table_info"] = ([vp, C.POINTER(TableInfo)], i32)
     sig["einspline_gb300_copy_table"] = ([vp, vp, vp], i32)
+    sig["einspline_gb300_host_coefs"] = ([vp, C.POINTER(vp)], i32)
+    sig["einspline_gb300_push_host_coefs"] = ([vp], i32)
+    sig["einspline_gb300_release_host_coefs"] = ([vp], i32)
     sig["einspline_gb300_eval_3d"] = ([vp, C.POINTER(EvalOpts), i64, vp, vp, vp, vp, vp], i32)
     sig["einspline_gb300_eval_3d_host"] = ([vp, C.POINTER(EvalOpts), i64, vp, vp, vp, vp], i32)
     sig["einspline_gb300_eval_3d_sorted_noalloc"] = ([vp, C.POINTER(EvalOpts), i64, vp, vp, vp, vp, vp], i32)

@@ -107,6 +107,31 @@ class MultiUBspline3D:
         check()
         return out, sc
 
+    def host_coefs(self) -> np.ndarray:
+        """The coefficients in host memory as the reference keeps them: a
+        numpy view [Nx][Ny][Nz][ncol_pad] of the library's pinned mirror, in
+        the value's real type (float32 for s/c, float64 for d/z; 16-bit
+        tables dequantized).  Edits reach the device table through
+        push_host_coefs (FP32 and FP64 tables)."""
+        ti = self.info()
+        p = C.c_void_p()
+        _lib().einspline_gb300_host_coefs(self.table, C.byref(p))
+        check()
+        dt = np.float64 if self.kind in "dz" else np.float32
+        n = ti.nx * ti.ny * ti.nz * ti.ncol_pad
+        buf = (C.c_char * (n * np.dtype(dt).itemsize)).from_address(p.value)
+        return np.frombuffer(buf, dtype=dt).reshape(ti.nx, ti.ny, ti.nz, ti.ncol_pad)
+
+    def push_host_coefs(self) -> None:
+        """Upload the host mirror (after edits) into the device table."""
+        _lib().einspline_gb300_push_host_coefs(self.table)
+        check()
+
+    def release_host_coefs(self) -> None:
+        """Free the host mirror; views from host_coefs become invalid."""
+        _lib().einspline_gb300_release_host_coefs(self.table)
+        check()
+
     def table_values(self) -> np.ndarray:
         """Dequantized table as float64 [Nx][Ny][Nz][N] (complex: [..., N, 2])."""
         t, sc = self.table_host()

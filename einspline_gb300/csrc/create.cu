@@ -2,6 +2,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <cuda_fp16.h>
+
 #include "eg_internal.h"
 
 using namespace eg;
@@ -437,6 +439,88 @@ int einspline_gb300_get_table_info(einspline_gb300_table *t, einspline_gb300_tab
   o->table_bytes = t->table_bytes;
   o->coefs = t->coefs;
   o->scale = t->scale;
+  return 0;
+}
+
+}  // extern "C"
+
+namespace {
+// Stored 16-bit reals times their column's factor, into the mirror's floats
+// (written through its mapped device address): row r of the table, column c.
+__global__ void k_dequant(const unsigned short *__restrict__ tab, const float *__restrict__ scale, int storage,
+                          int ncol, int ncol_pad, int64_t rows, float *__restrict__ out) {
+  const int64_t n = rows * ncol_pad;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % ncol_pad);
+    const unsigned short u = tab[i];
+    float v;
+    if (storage == ST_F16) v = __half2float(__ushort_as_half(u));
+    else if (storage == ST_BF16) v = __uint_as_float((unsigned)u << 16);
+    else v = (float)((int)u - kI16Bias);
+    out[i] = c < ncol ? v * scale[c] : 0.f;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int einspline_gb300_host_coefs(einspline_gb300_table *t, void **coefs_out) {
+  clear();
+  if (!table_ok(t) || !coefs_out) return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_host_coefs: bad argument");
+  if (int r = table_flush(t)) return r;
+  std::lock_guard<std::mutex> g(t->mu);
+  const bool narrow = t->storage == ST_F16 || t->storage == ST_BF16 || t->storage == ST_I16;
+  const size_t reals = t->table_bytes / t->elem_bytes;
+  const size_t bytes = reals * (narrow ? sizeof(float) : (size_t)t->elem_bytes);
+  if (!t->host_coefs) {
+    if (cudaHostAlloc(&t->host_coefs, bytes, cudaHostAllocMapped) != cudaSuccess) {
+      cudaGetLastError();
+      t->host_coefs = nullptr;
+      return fail(EINSPLINE_GB300_ENOMEM, "einspline_gb300_host_coefs: cannot allocate %zu bytes of host memory",
+                  bytes);
+    }
+    t->host_coefs_bytes = bytes;
+  }
+  EG_CUDA(cudaStreamSynchronize(t->stream));
+  if (narrow) {
+    void *dev = nullptr;
+    EG_CUDA(cudaHostGetDevicePointer(&dev, t->host_coefs, 0));
+    const int64_t rows = (int64_t)(reals / t->ncol_pad);
+    k_dequant<<<2048, 256, 0, t->stream>>>((const unsigned short *)t->coefs, t->scale, t->storage, t->ncol,
+                                          t->ncol_pad, rows, (float *)dev);
+    count_launch();
+    EG_CUDA(cudaGetLastError());
+    EG_CUDA(cudaStreamSynchronize(t->stream));
+  } else {
+    EG_CUDA(cudaMemcpy(t->host_coefs, t->coefs, bytes, cudaMemcpyDeviceToHost));
+  }
+  *coefs_out = t->host_coefs;
+  return 0;
+}
+
+int einspline_gb300_push_host_coefs(einspline_gb300_table *t) {
+  clear();
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_push_host_coefs: bad table handle");
+  if (!t->host_coefs)
+    return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_push_host_coefs: no host mirror (einspline_gb300_host_coefs)");
+  if (t->storage == ST_F16 || t->storage == ST_BF16 || t->storage == ST_I16)
+    return fail(EINSPLINE_GB300_EINVAL,
+                "einspline_gb300_push_host_coefs: 16-bit tables are built from data by set_* (their mirror is read-only)");
+  if (int r = table_flush(t)) return r;
+  std::lock_guard<std::mutex> g(t->mu);
+  EG_CUDA(cudaStreamSynchronize(t->stream));
+  EG_CUDA(cudaMemcpy(t->coefs, t->host_coefs, t->table_bytes, cudaMemcpyHostToDevice));
+  t->df_stale = true;  // a double-float copy is rebuilt before its next use
+  return 0;
+}
+
+int einspline_gb300_release_host_coefs(einspline_gb300_table *t) {
+  clear();
+  if (!table_ok(t)) return fail(EINSPLINE_GB300_EINVAL, "einspline_gb300_release_host_coefs: bad table handle");
+  std::lock_guard<std::mutex> g(t->mu);
+  if (t->host_coefs) cudaFreeHost(t->host_coefs);
+  t->host_coefs = nullptr;
+  t->host_coefs_bytes = 0;
   return 0;
 }
 

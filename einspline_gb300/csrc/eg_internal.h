@@ -128,6 +128,11 @@ struct einspline_gb300_table {
   // read/write mapped pinned host buffers directly
   int host_direct = 0;
 
+  // host mirror of the coefficients in the value type (einspline_gb300_host_coefs):
+  // pinned, mapped host memory of table_bytes / elem_bytes reals
+  void *host_coefs = nullptr;
+  size_t host_coefs_bytes = 0;
+
   // cell-sorted evaluation scratch
   void *sort_dev = nullptr;
   size_t sort_bytes = 0;

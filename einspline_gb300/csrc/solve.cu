@@ -536,6 +536,7 @@ void table_destroy(Table *t) {
   cudaFree(t->df_coefs);
   cudaFree(t->factors_d);
   if (t->pt_host) cudaFreeHost(t->pt_host);  // pt_dev is its device address
+  if (t->host_coefs) cudaFreeHost(t->host_coefs);
   if (t->wait_err_h) cudaFreeHost(t->wait_err_h);
   cudaFree(t->pipe_dev);
   cudaFree(t->sort_dev);

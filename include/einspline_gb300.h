@@ -105,6 +105,20 @@ int einspline_gb300_get_table_info(einspline_gb300_table *t, einspline_gb300_tab
 /* Copy the stored table (padded layout, storage type) to host memory of
  * table_bytes bytes; the scales (ncol floats) too when scale_host != NULL. */
 int einspline_gb300_copy_table(einspline_gb300_table *t, void *host_dst, float *scale_host);
+/* For callers that read or write spline->coefs on the host, as the
+ * reference's host table allows (src/multi_bspline_structs.h:155-164: coefs
+ * is host memory there; checkpoint reads and writes, broadcasts): a pinned
+ * host mirror of the coefficients in the reference's layout and value type
+ * (float for s/c, double for d/z; the struct's x/y/z strides apply),
+ * refreshed from the device table by each call (16-bit tables dequantised);
+ * *coefs_out may be stored in spline->coefs for such code.  After host
+ * edits, push_host_coefs uploads the mirror into the device table (FP32 and
+ * FP64 storage; EINVAL for 16-bit tables, which set_* builds from data);
+ * evaluation always reads the device table.  The mirror lives until
+ * release_host_coefs or the spline's destruction. */
+int einspline_gb300_host_coefs(einspline_gb300_table *t, void **coefs_out);
+int einspline_gb300_push_host_coefs(einspline_gb300_table *t);
+int einspline_gb300_release_host_coefs(einspline_gb300_table *t);
 
 /* ------------------------------------------------------------ evaluation */
 typedef struct {

@@ -7,8 +7,10 @@
  * its name, type and offset.  Two differences a caller must know:
  *   * coefs is a DEVICE pointer: the table lives in GPU memory (HBM) as
  *     coefs[Nx][Ny][Nz][z_stride].  Use einspline_gb300_copy_table() to read
- *     it on the host.  The storage type may be narrower than the value type
- *     for s/c tables made with einspline_gb300_create_3d_{s,c}.
+ *     it on the host, or einspline_gb300_host_coefs() for a host mirror in
+ *     the reference's layout and value type (pushed back to the device by
+ *     einspline_gb300_push_host_coefs()).  The storage type may be narrower
+ *     than the value type for s/c tables made with einspline_gb300_create_3d_{s,c}.
  *   * a private pointer (gb300) is appended after the public fields.  The
  *     structs are only ever made by this library's create functions, as in
  *     the reference, so appending does not change any public offset.
