@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
   const unsigned b_s = a_s + NS * kStage;
   // mbarriers: full/empty per stage; weight matrix full/empty, accumulator
   // full/empty per buffer; then the TMEM address, the abort flag and the
-  // count of points whose stencil the MMA warp consumed
+  // count of stencil stages the MMA warp consumed
   const unsigned full_s = b_s + 2 * 4096u, empty_s = full_s + 8 * NS, bfull_s = empty_s + 8 * NS;
   const unsigned bempty_s = bfull_s + 16, tfull_s = bempty_s + 16, tempty_s = tfull_s + 16, slot_s = tempty_s + 16;
   unsigned char *bgen = smem + (b_s - base_s);
