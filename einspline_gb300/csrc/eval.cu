@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
 // spline's factor and the point's sign.  Results agree with the FMA kernels
 // to FP32 rounding (not bit for bit).
 // Warp roles, synchronised only through mbarriers: warp 0 (one lane) keeps
-// up to kTcStages stencil copies in flight, one stage per tile of a point;
+// up to TcCfg::stages stencil copies in flight, one stage per tile of a point;
 // warp 1 (one lane) issues a tile's MMAs once its stencil, the point's
 // weight matrix and a free accumulator are there, commits each tile to the
 // barrier that frees its stage and each point to those that free the weight
@@ -545,10 +545,11 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
 // Every wait is bounded and also ends once another role gave up (a shared
 // flag): a block that gave up sets a.wait_err, waits (again bounded) for its
 // copies and MMAs in flight, and frees its tensor memory.
-template <bool VGH>
+template <int ST, bool VGH>
 __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr int NS = kTcStages, T = kTcTiles;
+  constexpr int NS = TcCfg<ST>::stages, NP = TcCfg<ST>::parts, T = kTcTiles;
+  constexpr unsigned kB = NP * 2048u;  // bytes of a weight matrix
   constexpr unsigned kStage = 16384u, kAcc = T * kTcN;  // bytes of a stage (one tile), TMEM columns per accumulator
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tile = blockIdx.x % a.ntiles;
@@ -579,13 +580,13 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
   // mbarriers: full/empty per stage; weight matrix full/empty, accumulator
   // full/empty per buffer; then the TMEM address, the abort flag and the
   // count of stencil stages the MMA warp consumed
-  const unsigned full_s = b_s + 2 * 4096u, empty_s = full_s + 8 * NS, bfull_s = empty_s + 8 * NS;
+  const unsigned full_s = b_s + 2 * kB, empty_s = full_s + 8 * NS, bfull_s = empty_s + 8 * NS;
   const unsigned bempty_s = bfull_s + 16, tfull_s = bempty_s + 16, tempty_s = tfull_s + 16, slot_s = tempty_s + 16;
   unsigned char *bgen = smem + (b_s - base_s);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + (slot_s + 4 - base_s));
   volatile int *consumed = reinterpret_cast<volatile int *>(smem + (slot_s + 8 - base_s));
   // weight columns 10..15 (and all but 0 for value only) stay zero
-  for (int e = tid; e < 2 * 4096 / 16; e += kTcThreads) reinterpret_cast<uint4 *>(bgen)[e] = make_uint4(0, 0, 0, 0);
+  for (int e = tid; e < 2 * (int)kB / 16; e += kTcThreads) reinterpret_cast<uint4 *>(bgen)[e] = make_uint4(0, 0, 0, 0);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_s), "n"(2 * kAcc)
                  : "memory");
@@ -642,8 +643,8 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMAs: per tile, the four x-planes against the high, then the low weights
-      constexpr uint32_t idesc = umma_idesc_f16(128, kTcN);
+      // MMAs: per tile, the four x-planes against each part of the weights
+      constexpr uint32_t idesc = umma_idesc_16(128, kTcN, TcCfg<ST>::fmt);
       bool go = true;
       for (int p = 0; p < pn && go; p++) {
         const int bb = p & 1;
@@ -656,11 +657,11 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
           *consumed = u + 1;
           tc_fence_after();
 #pragma unroll
-          for (int h = 0; h < 2; h++)
+          for (int h = 0; h < NP; h++)
 #pragma unroll
             for (int i = 0; i < 4; i++)
               umma_f16(tmem + bb * kAcc + t * kTcN, umma_desc(a_s + s * kStage + i * 2048u, 8192u, 1024u, 2),
-                       umma_desc(b_s + bb * 4096u + (h * 4 + i) * 512u, 128u, 256u, 0), idesc, h > 0 || i > 0);
+                       umma_desc(b_s + bb * kB + (h * 4 + i) * 512u, 128u, 256u, 0), idesc, h > 0 || i > 0);
           umma_commit(empty_s + 8 * s);
           last_commit = p;
         }
@@ -700,7 +701,7 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
     // Weight matrix of point p into buffer p & 1, then arrive on its barrier.
     auto build_b = [&](int p) {
       const float *w = sw + p * 36;
-      unsigned char *bm = bgen + (p & 1) * 4096 + boff;
+      unsigned char *bm = bgen + (p & 1) * kB + boff;
       // the nine basis weights of this stencil row (value, d1, d2 per axis)
       float wx[3], wy[3], wz[3];
 #pragma unroll
@@ -709,14 +710,27 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
         wy[d] = w[12 + 4 * d + kj];
         wz[d] = w[24 + 4 * d + km];
       }
-      // weight of output q at this row: f16 high part in the high tiles, low part in the low tiles
+      // weight of output q at this row, split into the parts' tiles: f16 high
+      // and low parts; bf16 high, middle and low parts (each remainder is
+      // exact in FP32, and the three parts sum to the weight exactly)
       auto put = [&](auto qc) {
         constexpr int q = decltype(qc)::value;
         const float wq = wx[OA[q]] * wy[OB[q]] * wz[OC[q]];
-        const __half hi = __float2half_rn(wq);
-        const __half lo = __float2half_rn(wq - __half2float(hi));
-        *reinterpret_cast<__half *>(bm + (q >> 3) * 256 + (q & 7) * 16) = hi;
-        *reinterpret_cast<__half *>(bm + 2048 + (q >> 3) * 256 + (q & 7) * 16) = lo;
+        unsigned char *e = bm + (q >> 3) * 256 + (q & 7) * 16;
+        if constexpr (ST == ST_BF16) {
+          const __nv_bfloat16 hi = __float2bfloat16_rn(wq);
+          const float r1 = wq - __bfloat162float(hi);
+          const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+          const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+          *reinterpret_cast<__nv_bfloat16 *>(e) = hi;
+          *reinterpret_cast<__nv_bfloat16 *>(e + 2048) = mid;
+          *reinterpret_cast<__nv_bfloat16 *>(e + 4096) = lo;
+        } else {
+          const __half hi = __float2half_rn(wq);
+          const __half lo = __float2half_rn(wq - __half2float(hi));
+          *reinterpret_cast<__half *>(e) = hi;
+          *reinterpret_cast<__half *>(e + 2048) = lo;
+        }
       };
       if (!(et & 1)) {
         put(std::integral_constant<int, 0>());
@@ -961,8 +975,8 @@ static const void *kernel_for(int mode) {
     if constexpr (ST == ST_DF) {
       if (mode == 2 || mode == 3) return (const void *)k_eval_pipe_df<VGH>;
     } else {
-      if constexpr (ST == ST_F16)
-        if (mode == 5) return (const void *)k_eval_tc<VGH>;
+      if constexpr (ST == ST_F16 || ST == ST_BF16)
+        if (mode == 5) return (const void *)k_eval_tc<ST, VGH>;
       if (mode == 2) return (const void *)k_eval_pipe<ST, VGH, false>;
       if (mode == 3) return (const void *)k_eval_pipe<ST, VGH, (ST == ST_F16 || ST == ST_BF16 || ST == ST_I16)>;
     }
@@ -1047,9 +1061,10 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
   a.mode = mode >= 0 ? mode : pick_mode(t, vgh, a.perm != nullptr);
   const int ks = kernel_storage(t);
   if (a.mode >= 2 && ks == ST_F64) a.mode = 0;        // IEEE FP64 is FMA-bound: no pipeline variant
-  // tensor cores: F16 tables; one column a thread, so not the complex CPU
-  // layout, whose outputs interleave a spline's two columns
-  if (a.mode == 5 && (t->storage != ST_F16 || (a.is_complex && a.layout == 1))) a.mode = is16(t->storage) ? 3 : 2;
+  // tensor cores: F16 and BF16 tables; one column a thread, so not the
+  // complex CPU layout, whose outputs interleave a spline's two columns
+  if (a.mode == 5 && ((t->storage != ST_F16 && t->storage != ST_BF16) || (a.is_complex && a.layout == 1)))
+    a.mode = is16(t->storage) ? 3 : 2;
   if (a.mode == 3 && !is16(t->storage)) a.mode = 2;   // the wide variant is for 16-bit tables
   const int VW = elems_per_thread(t) * ((a.mode == 3 || (a.mode == 4 && is16(t->storage))) ? 2 : 1);
   a.ntiles = (a.ncol + tx * VW - 1) / (tx * VW);
@@ -1065,7 +1080,8 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
     a.ntiles = (a.ncol + kTcCols - 1) / kTcCols;
     a.wait_err = t->wait_err_d;
     if (int r = encode_table_map(t, a.coefs, 2, 64, &a.tmap, 4, CU_TENSOR_MAP_SWIZZLE_128B)) return r;
-    *smem = tc_smem(pb);
+    *smem = t->storage == ST_BF16 ? tc_smem(pb, TcCfg<ST_BF16>::parts, TcCfg<ST_BF16>::stages)
+                                  : tc_smem(pb, TcCfg<ST_F16>::parts, TcCfg<ST_F16>::stages);
   } else if (a.mode == 4) {
     ty = 1;
     // narrower tiles where the stage buffers would not fit in shared memory

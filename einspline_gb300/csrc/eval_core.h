@@ -612,10 +612,10 @@ __device__ __forceinline__ uint64_t umma_desc(unsigned addr, unsigned lbo, unsig
   return (uint64_t)((addr & 0x3FFFFu) >> 4) | (uint64_t)((lbo >> 4) & 0x3FFFu) << 16 |
          (uint64_t)((sbo >> 4) & 0x3FFFu) << 32 | (uint64_t)1 << 46 | (uint64_t)(swizzle & 7u) << 61;
 }
-// Instruction descriptor of a kind::f16 MMA: f16 A and B, f32 accumulator,
-// A MN-major, B K-major, shape M x N.
-__host__ __device__ constexpr uint32_t umma_idesc_f16(int M, int N) {
-  return (1u << 4) | (1u << 15) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor of a kind::f16 MMA: A and B both f16 (fmt 0) or
+// both bf16 (fmt 1), f32 accumulator, A MN-major, B K-major, shape M x N.
+__host__ __device__ constexpr uint32_t umma_idesc_16(int M, int N, uint32_t fmt) {
+  return (1u << 4) | (fmt << 7) | (fmt << 10) | (1u << 15) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 // D[tmem] (+)= A * B for one K = 16 step, issued by one thread.
 __device__ __forceinline__ void umma_f16(unsigned tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, bool acc) {
@@ -660,21 +660,29 @@ __device__ __forceinline__ void tmem_ld2(unsigned taddr, uint32_t (&r)[2]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Tensor-core evaluation (load mode 5).  A block owns kTcTiles tiles of 128
-// columns (each the M of one MMA).  Shared memory: the points' weights,
-// cells and sources; slack to align the operand area to 1024 bytes (the
-// 128-byte swizzle atom); kTcStages stencil buffers, each 64 rows x 128 f16
-// columns of one tile (16 KB, two 8 KB boxes of 64 columns); two weight buffers of
-// eight 16 x 16 K-major tiles (the f16 high parts of the four x-planes, then
-// the low parts: 4 KB); mbarriers (two per stage, two per weight buffer and
-// per accumulator); the TMEM address, an abort flag and a count.
-constexpr int kTcStages = 4;  // stencil stages, one 128-column tile of a point each
+// Tensor-core evaluation (load mode 5, F16 and BF16 tables).  A block owns
+// kTcTiles tiles of 128 columns (each the M of one MMA).  Shared memory: the
+// points' weights, cells and sources; slack to align the operand area to
+// 1024 bytes (the 128-byte swizzle atom); TcCfg::stages stencil buffers,
+// each 64 rows x 128 16-bit columns of one tile (16 KB, two 8 KB boxes of 64
+// columns); two weight buffers of TcCfg::parts x four 16 x 16 K-major tiles
+// (the weights' parts for the four x-planes: 2 KB a part); mbarriers (two
+// per stage, two per weight buffer and per accumulator); the TMEM address,
+// an abort flag and a count.
 constexpr int kTcTiles = 2;
 constexpr int kTcCols = 128 * kTcTiles;  // columns per block
 constexpr int kTcN = 16;                 // 10 outputs, padded to the MMA's N
 constexpr int kTcThreads = 192;          // copy warp, MMA warp, 4 weight/output warps
-__host__ __device__ __forceinline__ size_t tc_smem(int pb) {
-  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
+// Per table type: an FP32 weight is the sum of two f16 parts (22 bits) or of
+// three bf16 parts (exactly: 3 x 8 bits); the BF16 weight buffers' third
+// part is paid for with one stencil stage less, so both keep three blocks an SM.
+template <int ST> struct TcCfg {
+  static constexpr int parts = ST == ST_BF16 ? 3 : 2;
+  static constexpr int stages = ST == ST_BF16 ? 3 : 4;
+  static constexpr uint32_t fmt = ST == ST_BF16 ? 1u : 0u;
+};
+__host__ __device__ __forceinline__ size_t tc_smem(int pb, int parts, int stages) {
+  return smem_total(pb, 4) + 1024 + (size_t)stages * 16384 + 2 * (size_t)parts * 2048 + 16 * stages + 64 + 16;
 }
 
 }  // namespace eg

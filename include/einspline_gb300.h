@@ -200,11 +200,12 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  *      one copy brings the 4x4 stencil rows of a point's x-plane for the
  *      whole block, completion is tracked by mbarriers; 8 columns a thread
  *      for 16-bit tables, 4 for FP32, 2 for double-float (IEEE FP64 uses 0);
- *   5: F16 tables: the reduction runs on the tensor cores (tcgen05.mma):
+ *   5: F16 and BF16 tables: the reduction runs on the tensor cores (tcgen05.mma):
  *      a block of 128 threads owns 128 columns, one TMA copy per 64 columns
  *      brings a point's whole 4x4x4 stencil in the MMA operand layout, and
- *      the point's weights, split into f16 high and low parts, are the other
- *      operand; FP32 accumulation in tensor memory.  Results agree with the
+ *      the point's weights, split into f16 high and low parts (bf16 high,
+ *      middle and low parts for BF16 tables), are the other operand; FP32
+ *      accumulation in tensor memory.  Results agree with the
  *      other modes to FP32 rounding, not bit for bit.  It is the default of
  *      vgh on F16 tables, whose vgh autotuning only tunes its points per
  *      block, so tuning changes no result.  Other tables, and complex tables

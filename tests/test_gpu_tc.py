@@ -1,7 +1,8 @@
-"""Load mode 5: F16 tables reduced on the tensor cores (tcgen05.mma with the
-stencil as the MN-major operand and the point's weights, split into f16
-high and low parts, as the other).  The products are exact and the sums
-FP32, so the results agree with the FMA kernels to FP32 rounding (held to
+"""Load mode 5: F16 and BF16 tables reduced on the tensor cores (tcgen05.mma
+with the stencil as the MN-major operand and the point's weights, split into
+f16 high and low parts or bf16 high, middle and low parts, as the other).
+The products are exact and the sums FP32, so the results agree with the FMA
+kernels to FP32 rounding (held to
 the FP32 parity tolerance, max |diff| / max |ref| per quantity), for every
 boundary condition, output form, partial last tile, point order and entry
 point; tables it does not serve fall back to their copy pipeline, bit for
@@ -38,13 +39,14 @@ def same(a, b, what):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16])
 @pytest.mark.parametrize("kind", "sc")
 @pytest.mark.parametrize("bcase", ["periodic", "mixed"])
 @pytest.mark.parametrize("nspl", [45, 300])
-def test_tc_matches_fma_kernels(orc, kind, bcase, nspl):
+def test_tc_matches_fma_kernels(orc, kind, bcase, nspl, storage):
     grids, bcs = (PERIODIC_UNIT, [(P, P)] * 3) if bcase == "periodic" else MIXED
     # 45 splines: one partial tile; 300 (600 complex columns): several, the last partial
-    G, T, _ = build_pair(orc, kind, grids, bcs, nspl, seed=801, storage=api.STORE_F16)
+    G, T, _ = build_pair(orc, kind, grids, bcs, nspl, seed=801, storage=storage)
     lo, hi = table_box(grids)
     pt = tpos(synth.points_uniform(802, 700, lo, hi))
     for vgh in (True, False):
@@ -64,13 +66,14 @@ def test_tc_matches_fma_kernels(orc, kind, bcase, nspl):
 
 
 @pytest.mark.gpu
-def test_tc_sorted_many_points_and_last_wave(orc):
-    """1024 F16 splines (eight 128-column tiles), 60,000 points: several
+@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16])
+def test_tc_sorted_many_points_and_last_wave(orc, storage):
+    """1024 splines (four 256-column blocks), 60,000 points: several
     waves, so the last wave's points go to shorter blocks; random and
     cell-sorted order give the same results (each point's arithmetic does
     not depend on its block), close to the FMA kernels."""
     grids = [(0.0, 1.0, 10)] * 3
-    G, T, _ = build_pair(orc, "s", grids, [(P, P)] * 3, 1024, seed=811, storage=api.STORE_F16)
+    G, T, _ = build_pair(orc, "s", grids, [(P, P)] * 3, 1024, seed=811, storage=storage)
     pt = tpos(synth.points_uniform(812, 60000))
     ref = run(G, pt, 3, (32, 1, 8))
     tc = run(G, pt, 5, (128, 1, 8))
@@ -131,11 +134,10 @@ def test_tc_reference_entries_and_server(orc):
 
 @pytest.mark.gpu
 def test_tc_other_tables_fall_back(orc):
-    """FP32, BF16, I16 and FP64 tables take their usual kernels when mode 5
-    is asked for: results bit-identical to those kernels."""
+    """FP32, I16 and FP64 tables take their usual kernels when mode 5 is
+    asked for: results bit-identical to those kernels."""
     grids = [(0.0, 1.0, 9)] * 3
-    for kind, storage, fb in (("s", api.STORE_F32, 2), ("s", api.STORE_BF16, 3), ("s", api.STORE_I16, 3),
-                              ("d", api.STORE_NATIVE, 0)):
+    for kind, storage, fb in (("s", api.STORE_F32, 2), ("s", api.STORE_I16, 3), ("d", api.STORE_NATIVE, 0)):
         G, T, _ = build_pair(orc, kind, grids, [(P, P)] * 3, 33, seed=831, storage=storage)
         pt = tpos(synth.points_uniform(832, 500))
         same(run(G, pt, 5, (128, 1, 8)), run(G, pt, fb, (128, 1, 8)), (kind, storage))

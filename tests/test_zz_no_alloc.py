@@ -28,13 +28,15 @@ def _call(lib, G, opts, npts, pos, out):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", "sd")
-def test_noalloc_sorted_matches_allocating_entry(kind):
+@pytest.mark.parametrize("kind,storage", [("s", api.STORE_NATIVE), ("d", api.STORE_NATIVE), ("s", api.STORE_F16)])
+def test_noalloc_sorted_matches_allocating_entry(kind, storage):
+    """FP32 and FP64 tables, and an F16 table, which evaluates on the tensor
+    cores (their tensor memory is on-chip, not device memory)."""
     import torch
     lib = L.load()
     M, N = 24, 96
     grids = [(0.0, 1.0, M)] * 3
-    G = api.MultiUBspline3D(kind, grids, [(api.PERIODIC, api.PERIODIC)] * 3, N)
+    G = api.MultiUBspline3D(kind, grids, [(api.PERIODIC, api.PERIODIC)] * 3, N, storage=storage)
     data = synth.grid_data_uniform(7, (M, M, M), N, np.float32 if kind == "s" else np.float64)
     for i in range(N):
         G.set(i, data[i])
