@@ -574,10 +574,10 @@ static int tune_shapes(Table *t, const EvalArgs &a, bool vgh, int best_shape[4])
     if (is16(ks)) modes.push_back(3);
     modes.push_back(4);
   }
-  // F16 vgh uses the tensor-core reduction (mode 5), whose results differ
-  // from the other modes' by FP32 rounding: only its points per block are
-  // tuned, so tuning never changes a result.
-  if (ks == ST_F16 && vgh) modes = {5};
+  // F16 and BF16 vgh use the tensor-core reduction (mode 5), whose results
+  // differ from the other modes' by FP32 rounding: only its points per block
+  // are tuned, so tuning never changes a result.
+  if ((ks == ST_F16 || ks == ST_BF16) && vgh) modes = {5};
   int rc = 0;
   for (int pf : modes) {
     t->tile_mode = pf;

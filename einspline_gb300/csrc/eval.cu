@@ -518,23 +518,26 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
   }
 }
 
-// Tensor-core evaluation (load mode 5, F16 tables).  For one point the ten
-// outputs of a column are a product of the point's 10 x 64 stencil weights
-// with the column's 64 stencil coefficients, so for each 128-column tile of
-// its kTcCols columns a block computes, point after point of its group,
-//   D[128 columns x 16] = A[128 columns x 64 rows] * B[64 rows x 16]
-// with tcgen05.mma (M 128, N 16, K 16) into an f32 accumulator in tensor
-// memory.  A is the stencil exactly as stored: TMA boxes of 64 columns x 4 z
-// x 4 y x 4 x in the 128-byte swizzle, which is the MN-major operand
-// layout.  B holds each output's weight w_x w_y w_z (FP32, without the
-// delta_inv factors) split into f16 high and low parts: eight K steps per
-// tile, the four x-planes against the high parts and again against the low
-// parts, so each output accumulates the exact products of its 22-bit weight
-// in one FP32 column; it is then scaled by its delta_inv factors, the
-// spline's factor and the point's sign.  Results agree with the FMA kernels
-// to FP32 rounding (not bit for bit).
+// Tensor-core evaluation (load mode 5, F16 and BF16 tables).  For one point
+// the ten outputs of a column are a product of the point's 10 x 64 stencil
+// weights with the column's 64 stencil coefficients, so for each 128-column
+// tile of its kTcCols columns a block computes, point after point of its
+// group,
+//   D[128 columns x 32] = A[128 columns x 64 rows] * B[64 rows x 32]
+// with four tcgen05.mma (M 128, N 32, K 16: one per x-plane) into f32
+// accumulators in tensor memory.  A is the stencil exactly as stored: TMA
+// boxes of 64 columns x 4 z x 4 y x 4 x in the 128-byte swizzle, which is
+// the MN-major operand layout.  B holds each output's weight w_x w_y w_z
+// (FP32, without the delta_inv factors) split into parts of the table's
+// type, each part in its own column: f16 high and low parts (22 bits), or
+// bf16 high, middle and low parts (the weight exactly).  The products are
+// exact and each column sums them in FP32; the epilogue adds an output's
+// columns and scales the sum by its delta_inv factors, the spline's factor
+// and the point's sign.  Results agree with the FMA kernels to FP32
+// rounding (not bit for bit).  Four MMAs per tile, not one per x-plane and
+// part: the MMA issue rate, not the math, bounded the cell-sorted case.
 // Warp roles, synchronised only through mbarriers: warp 0 (one lane) keeps
-// up to TcCfg::stages stencil copies in flight, one stage per tile of a point;
+// up to kTcStages stencil copies in flight, one stage per tile of a point;
 // warp 1 (one lane) issues a tile's MMAs once its stencil, the point's
 // weight matrix and a free accumulator are there, commits each tile to the
 // barrier that frees its stage and each point to those that free the weight
@@ -548,8 +551,8 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
 template <int ST, bool VGH>
 __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ EvalArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  constexpr int NS = TcCfg<ST>::stages, NP = TcCfg<ST>::parts, T = kTcTiles;
-  constexpr unsigned kB = NP * 2048u;  // bytes of a weight matrix
+  constexpr int NS = kTcStages, NP = TcCfg<ST>::parts, T = kTcTiles;
+  constexpr unsigned kB = 4096u;  // bytes of a weight matrix: four 32 x 16 tiles
   constexpr unsigned kStage = 16384u, kAcc = T * kTcN;  // bytes of a stage (one tile), TMEM columns per accumulator
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tile = blockIdx.x % a.ntiles;
@@ -657,11 +660,9 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
           *consumed = u + 1;
           tc_fence_after();
 #pragma unroll
-          for (int h = 0; h < NP; h++)
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-              umma_f16(tmem + bb * kAcc + t * kTcN, umma_desc(a_s + s * kStage + i * 2048u, 8192u, 1024u, 2),
-                       umma_desc(b_s + bb * kB + (h * 4 + i) * 512u, 128u, 256u, 0), idesc, h > 0 || i > 0);
+          for (int i = 0; i < 4; i++)
+            umma_f16(tmem + bb * kAcc + t * kTcN, umma_desc(a_s + s * kStage + i * 2048u, 8192u, 1024u, 2),
+                     umma_desc(b_s + bb * kB + i * 1024u, 128u, 256u, 0), idesc, i > 0);
           umma_commit(empty_s + 8 * s);
           last_commit = p;
         }
@@ -678,7 +679,7 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
     // (even threads) or 5-9 (odd threads)
     const int k = et >> 1;
     const int ki = k >> 4, kj = (k >> 2) & 3, km = k & 3, kk = k & 15;
-    const unsigned boff = ki * 512 + (kk >> 3) * 128 + (kk & 7) * 2;
+    const unsigned boff = ki * 1024 + (kk >> 3) * 128 + (kk & 7) * 2;
     // derivative orders in x, y, z of each output (v, gx, gy, gz, hxx, hxy, hxz, hyy, hyz, hzz)
     static constexpr int OA[10] = {0, 1, 0, 0, 2, 1, 1, 0, 0, 0};
     static constexpr int OB[10] = {0, 0, 1, 0, 0, 1, 0, 2, 1, 0};
@@ -716,20 +717,20 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
       auto put = [&](auto qc) {
         constexpr int q = decltype(qc)::value;
         const float wq = wx[OA[q]] * wy[OB[q]] * wz[OC[q]];
-        unsigned char *e = bm + (q >> 3) * 256 + (q & 7) * 16;
+        auto at = [&](int n) { return bm + (n >> 3) * 256 + (n & 7) * 16; };
         if constexpr (ST == ST_BF16) {
           const __nv_bfloat16 hi = __float2bfloat16_rn(wq);
           const float r1 = wq - __bfloat162float(hi);
           const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
           const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
-          *reinterpret_cast<__nv_bfloat16 *>(e) = hi;
-          *reinterpret_cast<__nv_bfloat16 *>(e + 2048) = mid;
-          *reinterpret_cast<__nv_bfloat16 *>(e + 4096) = lo;
+          *reinterpret_cast<__nv_bfloat16 *>(at(3 * q)) = hi;
+          *reinterpret_cast<__nv_bfloat16 *>(at(3 * q + 1)) = mid;
+          *reinterpret_cast<__nv_bfloat16 *>(at(3 * q + 2)) = lo;
         } else {
           const __half hi = __float2half_rn(wq);
           const __half lo = __float2half_rn(wq - __half2float(hi));
-          *reinterpret_cast<__half *>(e) = hi;
-          *reinterpret_cast<__half *>(e + 2048) = lo;
+          *reinterpret_cast<__half *>(at(2 * q)) = hi;
+          *reinterpret_cast<__half *>(at(2 * q + 1)) = lo;
         }
       };
       if (!(et & 1)) {
@@ -760,12 +761,22 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
       const int bb = p & 1;
       if (!wait(tfull_s + 8 * bb, (unsigned)((p >> 1) & 1))) break;
       tc_fence_after();
-      uint32_t r[32];
-      static_assert(T * kTcN <= 32, "one load reads every tile's accumulator");
-      if constexpr (T * kTcN == 32) tmem_ld32(tmem + ((unsigned)((warp & 3) * 32) << 16) + bb * kAcc, r);
-      else tmem_ld16(tmem + ((unsigned)((warp & 3) * 32) << 16) + bb * kAcc, r);
+      uint32_t rr[T][32];
+#pragma unroll
+      for (int t = 0; t < T; t++) tmem_ld32(tmem + ((unsigned)((warp & 3) * 32) << 16) + bb * kAcc + t * kTcN, rr[t]);
       tc_fence_before();
       mbar_arrive(tempty_s + 8 * bb);
+      // each output: the sum of its weight parts' columns
+      uint32_t r[T * 16];
+#pragma unroll
+      for (int t = 0; t < T; t++)
+#pragma unroll
+        for (int q = 0; q < 10; q++) {
+          float v = __uint_as_float(rr[t][NP * q]);
+#pragma unroll
+          for (int h = 1; h < NP; h++) v += __uint_as_float(rr[t][NP * q + h]);
+          r[t * 16 + q] = __float_as_uint(v);
+        }
       const int64_t src = ssrc[p];
       if (plain) {
         // flat GPU layout: value, 3 gradient and 6 Hessian reals per column
@@ -778,7 +789,7 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
           if (col >= a.ncol) continue;
           float o[10];
 #pragma unroll
-          for (int q = 0; q < 10; q++) o[q] = __uint_as_float(r[t * kTcN + q]) * f[t][q];
+          for (int q = 0; q < 10; q++) o[q] = __uint_as_float(r[t * 16 + q]) * f[t][q];
           vp[col] = o[0];
 #pragma unroll
           for (int c = 0; c < 3; c++) gp[3 * col + c] = o[1 + c];
@@ -793,7 +804,7 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
         if (col >= a.ncol) continue;
         float o[10][1];
 #pragma unroll
-        for (int q = 0; q < (VGH ? 10 : 1); q++) o[q][0] = __uint_as_float(r[t * kTcN + q]) * f[t][q];
+        for (int q = 0; q < (VGH ? 10 : 1); q++) o[q][0] = __uint_as_float(r[t * 16 + q]) * f[t][q];
         epilogue<float, 1, VGH, false>(a, src, col, o);
       }
     }
@@ -1080,8 +1091,7 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
     a.ntiles = (a.ncol + kTcCols - 1) / kTcCols;
     a.wait_err = t->wait_err_d;
     if (int r = encode_table_map(t, a.coefs, 2, 64, &a.tmap, 4, CU_TENSOR_MAP_SWIZZLE_128B)) return r;
-    *smem = t->storage == ST_BF16 ? tc_smem(pb, TcCfg<ST_BF16>::parts, TcCfg<ST_BF16>::stages)
-                                  : tc_smem(pb, TcCfg<ST_F16>::parts, TcCfg<ST_F16>::stages);
+    *smem = tc_smem(pb);
   } else if (a.mode == 4) {
     ty = 1;
     // narrower tiles where the stage buffers would not fit in shared memory
@@ -1228,11 +1238,12 @@ int pick_mode(Table *t, bool vgh, bool sorted) {
   const int v = vgh ? 1 : 0;
   if (sorted && t->tuned_s_tx[v]) return t->tuned_s_mode[v];
   if (t->tuned_tx[v]) return t->tuned_mode[v];
-  // F16 vgh: the tensor-core reduction (64^3 x 1024, 64 walkers: 45.0 G
-  // evals/s random and 54.1 G cell-sorted against 43.0 G and 44.6 G for the
-  // wide copy pipeline); value only stays on the wide pipeline (58.4 G
-  // random and 90.9 G sorted against 57.8 G and 74.0 G)
-  if (vgh && t->storage == ST_F16) return 5;
+  // F16 and BF16 vgh: the tensor-core reduction (64^3 x 1024, 64 walkers:
+  // F16 45.5 G evals/s random and 64.6 G cell-sorted against 43.0 G and
+  // 44.6 G for the wide copy pipeline; BF16 45.5 G and 62.9 G against 42.9 G
+  // and 46.1 G); value only stays on the wide pipeline (58.4 G random and
+  // 90.9 G sorted against 57.8 G and 74.0 G for F16)
+  if (vgh && (t->storage == ST_F16 || t->storage == ST_BF16)) return 5;
   if (vgh && kernel_storage(t) != ST_F64) return is16(t->storage) ? 3 : 2;
   // value only: the wide pipeline for 16-bit tables (0.294 against 0.413 ms
   // with direct loads at 64^3 x 1024, 17k points); FP32 is as fast direct
@@ -1245,7 +1256,7 @@ void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb, bool
   const int v = vgh ? 1 : 0;
   if (sorted && t->tuned_s_tx[v]) { tx = t->tuned_s_tx[v]; ty = t->tuned_s_ty[v]; pb = t->tuned_s_pb[v]; return; }
   if (t->tuned_tx[v]) { tx = t->tuned_tx[v]; ty = t->tuned_ty[v]; pb = t->tuned_pb[v]; return; }
-  if (t->storage == ST_F16 && ((vgh && t->tile_mode < 0) || t->tile_mode == 5)) {
+  if ((t->storage == ST_F16 || t->storage == ST_BF16) && ((vgh && t->tile_mode < 0) || t->tile_mode == 5)) {
     // tensor cores: 10 points a block keep three blocks on an SM (74.7 KB of
     // shared memory each); the block's threads are fixed by the kernel
     tx = 128;

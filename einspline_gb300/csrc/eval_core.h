@@ -663,26 +663,26 @@ __device__ __forceinline__ void tmem_ld2(unsigned taddr, uint32_t (&r)[2]) {
 // Tensor-core evaluation (load mode 5, F16 and BF16 tables).  A block owns
 // kTcTiles tiles of 128 columns (each the M of one MMA).  Shared memory: the
 // points' weights, cells and sources; slack to align the operand area to
-// 1024 bytes (the 128-byte swizzle atom); TcCfg::stages stencil buffers,
+// 1024 bytes (the 128-byte swizzle atom); kTcStages stencil buffers,
 // each 64 rows x 128 16-bit columns of one tile (16 KB, two 8 KB boxes of 64
-// columns); two weight buffers of TcCfg::parts x four 16 x 16 K-major tiles
-// (the weights' parts for the four x-planes: 2 KB a part); mbarriers (two
-// per stage, two per weight buffer and per accumulator); the TMEM address,
-// an abort flag and a count.
+// columns); two weight buffers of four 32 x 16 K-major tiles, one per
+// x-plane (4 KB: output q's weight parts in columns parts * q + h);
+// mbarriers (two per stage, two per weight buffer and per accumulator); the
+// TMEM address, an abort flag and a count.
 constexpr int kTcTiles = 2;
 constexpr int kTcCols = 128 * kTcTiles;  // columns per block
-constexpr int kTcN = 16;                 // 10 outputs, padded to the MMA's N
+constexpr int kTcN = 32;                 // 10 outputs x weight parts (<= 3), padded to the MMA's N
 constexpr int kTcThreads = 192;          // copy warp, MMA warp, 4 weight/output warps
+constexpr int kTcStages = 4;             // stencil stages, one 128-column tile of a point each
 // Per table type: an FP32 weight is the sum of two f16 parts (22 bits) or of
-// three bf16 parts (exactly: 3 x 8 bits); the BF16 weight buffers' third
-// part is paid for with one stencil stage less, so both keep three blocks an SM.
+// three bf16 parts (exactly: 3 x 8 bits), each part accumulating in its own
+// column, summed in the epilogue.
 template <int ST> struct TcCfg {
   static constexpr int parts = ST == ST_BF16 ? 3 : 2;
-  static constexpr int stages = ST == ST_BF16 ? 3 : 4;
   static constexpr uint32_t fmt = ST == ST_BF16 ? 1u : 0u;
 };
-__host__ __device__ __forceinline__ size_t tc_smem(int pb, int parts, int stages) {
-  return smem_total(pb, 4) + 1024 + (size_t)stages * 16384 + 2 * (size_t)parts * 2048 + 16 * stages + 64 + 16;
+__host__ __device__ __forceinline__ size_t tc_smem(int pb) {
+  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
 }
 
 }  // namespace eg

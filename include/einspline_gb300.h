@@ -201,18 +201,18 @@ int einspline_gb300_get_tile(einspline_gb300_table *t, int *tx, int *ty, int *pb
  *      whole block, completion is tracked by mbarriers; 8 columns a thread
  *      for 16-bit tables, 4 for FP32, 2 for double-float (IEEE FP64 uses 0);
  *   5: F16 and BF16 tables: the reduction runs on the tensor cores (tcgen05.mma):
- *      a block of 128 threads owns 128 columns, one TMA copy per 64 columns
- *      brings a point's whole 4x4x4 stencil in the MMA operand layout, and
+ *      a block owns 256 columns, one TMA copy per 64 columns brings a
+ *      point's whole 4x4x4 stencil in the MMA operand layout, and
  *      the point's weights, split into f16 high and low parts (bf16 high,
  *      middle and low parts for BF16 tables), are the other operand; FP32
  *      accumulation in tensor memory.  Results agree with the
  *      other modes to FP32 rounding, not bit for bit.  It is the default of
- *      vgh on F16 tables, whose vgh autotuning only tunes its points per
- *      block, so tuning changes no result.  Other tables, and complex tables
- *      in the CPU layout, use their pipeline (3 or 2) instead;
- *  -1: the autotuned choice; untuned, vgh uses 5 for F16 tables, 3 for the
- *      other 16-bit tables and 2 for FP32 (the choices the autotuner makes
- *      on GB300); value-only uses 3 for 16-bit tables and 0 for FP32; FP64
+ *      vgh on F16 and BF16 tables, whose vgh autotuning only tunes its
+ *      points per block, so tuning changes no result.  Other tables, and
+ *      complex tables in the CPU layout, use their pipeline (3 or 2) instead;
+ *  -1: the autotuned choice; untuned, vgh uses 5 for F16 and BF16 tables, 3
+ *      for I16 tables and 2 for FP32 (the choices the autotuner makes on
+ *      GB300); value-only uses 3 for 16-bit tables and 0 for FP32; FP64
  *      uses 0.  Results are identical in modes 0-4, and within mode 5. */
 int einspline_gb300_set_load_mode(einspline_gb300_table *t, int mode);
 int einspline_gb300_get_load_mode(einspline_gb300_table *t);
