@@ -38,7 +38,7 @@ UNIT = "spline-evals/s"
 BYTES_F32 = 64 * 4 + 10 * 4   # algorithmic bytes per vgh spline-eval, FP32 table
 BYTES_F16 = 64 * 2 + 10 * 4   # FP16 table (per-spline scale amortised to 0)
 KERNEL_BY_MODE = {0: "k_eval<F16,vgh>", 1: "k_eval<F16,vgh> (L2 bulk prefetch)", 2: "k_eval_pipe<F16,vgh>",
-                  3: "k_eval_pipe<F16,vgh,wide>", 4: "k_eval_tma<F16,vgh>", 5: "k_eval_tc<vgh> (tensor cores)"}
+                  3: "k_eval_pipe<F16,vgh,wide>", 4: "k_eval_tma<F16,vgh>", 5: "k_eval_tc<F16,vgh> (tensor cores)"}
 # DRAM bytes per eval measured by ncu for the kernel of each load mode (profiles/traffic.json)
 TRAFFIC_KEY_BY_MODE = {3: "f16_vgh_bytes_per_eval", 5: "f16_vgh_tc_bytes_per_eval"}
 
