@@ -540,11 +540,13 @@ __global__ void __launch_bounds__(256) k_eval_tma(const __grid_constant__ EvalAr
 // up to kTcStages stencil copies in flight, one stage per tile of a point;
 // warp 1 (one lane) issues a tile's MMAs once its stencil, the point's
 // weight matrix and a free accumulator are there, commits each tile to the
-// barrier that frees its stage and each point to those that free the weight
-// buffer and fill the accumulator; warps 2-5 (each
-// the TMEM lanes of its quarter: one column of every tile a thread) build
-// the next point's weight matrix, then read this point's accumulator and
-// store its outputs.  Weight matrices and accumulators are double-buffered.
+// barrier that frees its stage and each point to the one that fills the
+// accumulator; warps 2-5 (each the TMEM lanes of its quarter: one column of
+// every tile a thread) read a point's accumulator, build the weight matrix
+// of the point two ahead in the buffer whose last reader was that point's
+// MMAs, then store the point's outputs, so that the stores are not on the
+// path from one point's MMAs to the next's.  Weight matrices and
+// accumulators are double-buffered.
 // Every wait is bounded and also ends once another role gave up (a shared
 // flag): a block that gave up sets a.wait_err, waits (again bounded) for its
 // copies and MMAs in flight, and frees its tensor memory.
@@ -580,11 +582,11 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
   const unsigned base_s = (unsigned)__cvta_generic_to_shared(smem);
   const unsigned a_s = (base_s + (unsigned)smem_total(a.pb, 4) + 1023u) & ~1023u;
   const unsigned b_s = a_s + NS * kStage;
-  // mbarriers: full/empty per stage; weight matrix full/empty, accumulator
+  // mbarriers: full/empty per stage; weight matrix full, accumulator
   // full/empty per buffer; then the TMEM address, the abort flag and the
   // count of stencil stages the MMA warp consumed
   const unsigned full_s = b_s + 2 * kB, empty_s = full_s + 8 * NS, bfull_s = empty_s + 8 * NS;
-  const unsigned bempty_s = bfull_s + 16, tfull_s = bempty_s + 16, tempty_s = tfull_s + 16, slot_s = tempty_s + 16;
+  const unsigned tfull_s = bfull_s + 16, tempty_s = tfull_s + 16, slot_s = tempty_s + 16;
   unsigned char *bgen = smem + (b_s - base_s);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + (slot_s + 4 - base_s));
   volatile int *consumed = reinterpret_cast<volatile int *>(smem + (slot_s + 8 - base_s));
@@ -604,7 +606,6 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
 #pragma unroll
     for (int b = 0; b < 2; b++) {
       mbar_init(bfull_s + 8 * b, 128);
-      mbar_init(bempty_s + 8 * b, 1);
       mbar_init(tfull_s + 8 * b, 1);
       mbar_init(tempty_s + 8 * b, 128);
     }
@@ -667,7 +668,6 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
           last_commit = p;
         }
         if (!go) break;
-        umma_commit(bempty_s + 8 * bb);
         umma_commit(tfull_s + 8 * bb);
       }
     }
@@ -752,14 +752,14 @@ __global__ void __launch_bounds__(kTcThreads) k_eval_tc(const __grid_constant__ 
       mbar_arrive(bfull_s + 8 * (p & 1));
     };
     build_b(0);
+    if (pn > 1) build_b(1);
     for (int p = 0; p < pn; p++) {
-      if (p + 1 < pn) {
-        // the weight buffer of point p + 1 was last read by the MMAs of point p - 1
-        if (p >= 1 && !wait(bempty_s + 8 * ((p + 1) & 1), (unsigned)((((p + 1) >> 1) - 1) & 1))) break;
-        build_b(p + 1);
-      }
       const int bb = p & 1;
       if (!wait(tfull_s + 8 * bb, (unsigned)((p >> 1) & 1))) break;
+      // the MMAs of point p, the last to read weight buffer bb, are
+      // complete: point p + 2's weights go there now, so that its MMAs wait
+      // on neither this point's stores nor their issue
+      if (p + 2 < pn) build_b(p + 2);
       tc_fence_after();
       uint32_t rr[T][32];
 #pragma unroll

@@ -667,8 +667,8 @@ __device__ __forceinline__ void tmem_ld2(unsigned taddr, uint32_t (&r)[2]) {
 // each 64 rows x 128 16-bit columns of one tile (16 KB, two 8 KB boxes of 64
 // columns); two weight buffers of four 32 x 16 K-major tiles, one per
 // x-plane (4 KB: output q's weight parts in columns parts * q + h);
-// mbarriers (two per stage, two per weight buffer and per accumulator); the
-// TMEM address, an abort flag and a count.
+// mbarriers (two per stage, one per weight buffer, two per accumulator);
+// the TMEM address, an abort flag and a count.
 constexpr int kTcTiles = 2;
 constexpr int kTcCols = 128 * kTcTiles;  // columns per block
 constexpr int kTcN = 32;                 // 10 outputs x weight parts (<= 3), padded to the MMA's N
@@ -682,7 +682,7 @@ template <int ST> struct TcCfg {
   static constexpr uint32_t fmt = ST == ST_BF16 ? 1u : 0u;
 };
 __host__ __device__ __forceinline__ size_t tc_smem(int pb) {
-  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * 16384 + 2 * 4096 + 16 * kTcStages + 64 + 16;
+  return smem_total(pb, 4) + 1024 + (size_t)kTcStages * 16384 + 2 * 4096 + 16 * kTcStages + 48 + 16;
 }
 
 }  // namespace eg
