@@ -299,6 +299,14 @@ static int eval_device(Table *t, const einspline_gb300_eval_opts *o, int64_t npt
   return launch_eval(t, a, o->vgh != 0, s, tx, ty, pb);
 }
 
+// n rows of `width` bytes from packed device rows into host rows `pitch`
+// bytes apart: one linear copy when the host rows are packed too (the usual
+// case), a strided one otherwise.
+cudaError_t copy_rows(char *dst, size_t pitch, const char *src, size_t width, int64_t n, cudaStream_t s) {
+  if (pitch == width) return cudaMemcpyAsync(dst, src, width * (size_t)n, cudaMemcpyDeviceToHost, s);
+  return cudaMemcpy2DAsync(dst, pitch, src, width, width, (size_t)n, cudaMemcpyDeviceToHost, s);
+}
+
 }  // namespace eg
 
 using namespace eg;
@@ -441,13 +449,10 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
     char *h_d = g_d + (size_t)chunk * 3 * t->ncol * rb;
     EG_CUDA(cudaMemcpyAsync(pos_d, (const char *)pos_h + p0 * pos_b, n * pos_b, cudaMemcpyHostToDevice, s));
     if (int r = eval_device(t, &od, n, pos_d, v_d, g_d, h_d, s)) return r;
-    EG_CUDA(cudaMemcpy2DAsync((char *)vals_h + p0 * vs * rb, vs * rb, v_d, t->ncol * rb, t->ncol * rb, n,
-                              cudaMemcpyDeviceToHost, s));
+    EG_CUDA(copy_rows((char *)vals_h + p0 * vs * rb, vs * rb, v_d, t->ncol * rb, n, s));
     if (o->vgh) {
-      EG_CUDA(cudaMemcpy2DAsync((char *)grads_h + p0 * gs * rb, gs * rb, g_d, 3 * t->ncol * rb, 3 * t->ncol * rb, n,
-                                cudaMemcpyDeviceToHost, s));
-      EG_CUDA(cudaMemcpy2DAsync((char *)hess_h + p0 * hs * rb, hs * rb, h_d, hq * t->ncol * rb, hq * t->ncol * rb, n,
-                                cudaMemcpyDeviceToHost, s));
+      EG_CUDA(copy_rows((char *)grads_h + p0 * gs * rb, gs * rb, g_d, 3 * t->ncol * rb, n, s));
+      EG_CUDA(copy_rows((char *)hess_h + p0 * hs * rb, hs * rb, h_d, hq * t->ncol * rb, n, s));
     }
   }
   EG_CUDA(cudaStreamSynchronize(t->pipe_stream[0]));

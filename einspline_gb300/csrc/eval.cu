@@ -1239,8 +1239,8 @@ int pick_mode(Table *t, bool vgh, bool sorted) {
   if (sorted && t->tuned_s_tx[v]) return t->tuned_s_mode[v];
   if (t->tuned_tx[v]) return t->tuned_mode[v];
   // F16 and BF16 vgh: the tensor-core reduction (64^3 x 1024, 64 walkers:
-  // F16 45.5 G evals/s random and 64.6 G cell-sorted against 43.0 G and
-  // 44.6 G for the wide copy pipeline; BF16 45.5 G and 62.9 G against 42.9 G
+  // F16 45.7 G evals/s random and 66.3 G cell-sorted against 43.0 G and
+  // 44.6 G for the wide copy pipeline; BF16 45.5 G and 64.4 G against 42.9 G
   // and 46.1 G); value only stays on the wide pipeline (58.4 G random and
   // 90.9 G sorted against 57.8 G and 74.0 G for F16)
   if (vgh && (t->storage == ST_F16 || t->storage == ST_BF16)) return 5;

@@ -29,7 +29,7 @@ def main():
     ap.add_argument("--tile", type=int, nargs=3, default=None)
     ap.add_argument("--sort", type=int, default=0)
     ap.add_argument("--mode", type=int, default=-1, help="load mode: 0 direct, 1 L2 prefetch, 2 smem pipeline, "
-                    "3 wide smem pipeline (16-bit), 4 TMA pipeline")
+                    "3 wide smem pipeline (16-bit), 4 TMA pipeline, 5 tensor cores (F16, BF16)")
     ap.add_argument("--sweep", type=int, default=0, help="time every tile shape in every load mode")
     ap.add_argument("--det", type=int, default=0,
                     help="W > 0: time the fused determinant ratio (value, gradient, Laplacian; transposed "

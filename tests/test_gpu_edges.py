@@ -82,6 +82,37 @@ def test_host_entry_with_strides(orc):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("pad", [0, 3])
+def test_host_entry_many_chunks(pad):
+    """1024 splines (about 1,600 points per 64 MB output chunk), 5,000
+    points: four chunks on the two pipeline streams, the last partial, into
+    packed host rows (one linear copy per output) or rows `pad` elements
+    longer (strided copies); bit-identical to the device entry."""
+    import torch
+    n, npts = 1024, 5000
+    G = api.MultiUBspline3D("s", [(0.0, 1.0, 8)] * 3, [(P, P)] * 3, n)
+    buf = torch.empty((n, 8, 8, 8), dtype=torch.float32, device="cuda")
+    api.fill_uniform(buf, 411, -1.0, 1.0)
+    G.set_device(0, buf)
+    G.flush()
+    pos = synth.points_uniform(412, npts)
+    ref = [x.cpu().numpy() for x in G.eval(torch.from_numpy(pos).cuda(), rule=0, layout=0)]
+    vs, gs, hs = n + pad, 3 * n + pad, 6 * n + pad
+    v = np.full((npts, vs), -5.0, np.float32)
+    g = np.full((npts, gs), -5.0, np.float32)
+    h = np.full((npts, hs), -5.0, np.float32)
+    o = L.EvalOpts(1, 1, 0, 0, 0, vs, gs, hs)
+    L.load().einspline_gb300_eval_3d_host(G.table, C.byref(o), npts, C.c_void_p(pos.ctypes.data),
+                                          C.c_void_p(v.ctypes.data), C.c_void_p(g.ctypes.data),
+                                          C.c_void_p(h.ctypes.data))
+    api.check()
+    assert np.array_equal(v[:, :n], ref[0])
+    assert np.array_equal(g[:, :3 * n].reshape(npts, n, 3), ref[1])
+    assert np.array_equal(h[:, :6 * n].reshape(npts, n, 6), ref[2])
+    assert (v[:, n:] == -5).all() and (g[:, 3 * n:] == -5).all() and (h[:, 6 * n:] == -5).all()
+
+
+@pytest.mark.gpu
 def test_argument_errors_on_gpu():
     lib = L.load()
     G = api.MultiUBspline3D("s", [(0.0, 1.0, 8)] * 3, [(P, P)] * 3, 4)
