@@ -415,9 +415,12 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
   const int hq = o->layout ? 9 : 6;
   const size_t per_pt_out = (size_t)t->ncol * rb * (o->vgh ? (4 + hq) : 1);
   const size_t pos_b = o->pos_f64 ? 24 : 12;
-  // Chunks of about 64 MB of output, two in flight.
-  int64_t chunk = std::max<int64_t>(1, (int64_t)((64u << 20) / per_pt_out));
+  // Chunks of output, two in flight: the first about 8 MB, so that the
+  // device-to-host link starts early, then doubling up to about 128 MB, so
+  // that few copies carry the rest (the link, ~193 GB/s, is the bound).
+  int64_t chunk = std::max<int64_t>(1, (int64_t)((128u << 20) / per_pt_out));
   chunk = std::min(chunk, npts);
+  int64_t cur = std::max<int64_t>(1, (int64_t)((8u << 20) / per_pt_out));
   const size_t slot = align_up_sz(chunk * pos_b, 256) + align_up_sz(chunk * per_pt_out, 256);
   if (t->pipe_bytes < 2 * slot) {
     cudaFree(t->pipe_dev);
@@ -438,8 +441,10 @@ int einspline_gb300_eval_3d_host(einspline_gb300_table *t, const einspline_gb300
   od.vstride = t->ncol; od.gstride = 3 * (int64_t)t->ncol; od.hstride = hq * (int64_t)t->ncol;
   od.sort = 0;
   int k = 0;
-  for (int64_t p0 = 0; p0 < npts; p0 += chunk, k++) {
-    const int64_t n = std::min(chunk, npts - p0);
+  int64_t n = 0;
+  for (int64_t p0 = 0; p0 < npts; p0 += n, k++) {
+    n = std::min(std::min(cur, chunk), npts - p0);
+    cur = std::min(2 * cur, chunk);
     cudaStream_t s = t->pipe_stream[k & 1];
     char *base = (char *)t->pipe_dev + (size_t)(k & 1) * slot;
     char *pos_d = base;

@@ -84,10 +84,11 @@ def test_host_entry_with_strides(orc):
 @pytest.mark.gpu
 @pytest.mark.parametrize("pad", [0, 3])
 def test_host_entry_many_chunks(pad):
-    """1024 splines (about 1,600 points per 64 MB output chunk), 5,000
-    points: four chunks on the two pipeline streams, the last partial, into
-    packed host rows (one linear copy per output) or rows `pad` elements
-    longer (strided copies); bit-identical to the device entry."""
+    """1024 splines (output chunks of about 200 points, then twice as many
+    each time up to about 3,300), 5,000 points: five chunks on the two
+    pipeline streams, the last partial, into packed host rows (one linear
+    copy per output) or rows `pad` elements longer (strided copies);
+    bit-identical to the device entry."""
     import torch
     n, npts = 1024, 5000
     G = api.MultiUBspline3D("s", [(0.0, 1.0, 8)] * 3, [(P, P)] * 3, n)
