@@ -232,6 +232,323 @@ __global__ void __launch_bounds__(kDetThreads, kDetBlocksPerSM) k_det_ratio(cons
   }
 }
 
+// ------------------------------------------------------------ tensor cores
+// k_det_tc: the ratio of F16 and BF16 tables in their default load mode 5,
+// with the evaluation kernel's tensor-core contraction (k_eval_tc, eval.cu):
+// per walker and tile of 128 orbitals, D[128 orbitals x NC] = A[128 x 64] *
+// B[64 x NC] in four tcgen05.mma (K = 16, one per x-plane), A the stencil as
+// a TMA box copies it (128-byte swizzle), B the walker's weights of seven
+// outputs (value, gradient, the Hessian's diagonal) split into the table
+// type's parts, each part in its own column.  Instead of storing the
+// outputs, the epilogue dots them with the inverse column.
+//
+// A block takes pb walkers and all N orbitals: unit u = p * TT + t is tile
+// t of walker p.  Warp 0 (one lane) keeps kDtStages stencil copies in
+// flight, one unit a stage; warp 1 (one lane) issues a unit's MMAs into
+// one of the block's accumulator slots (unit u into slot u modulo their
+// number) once its stencil, the walker's weights and the slot are there,
+// and commits the unit to the barriers that free its
+// stage and fill its slot; warps 2-5 (one orbital of each tile a thread)
+// read a slot, free it, add the weight parts, scale, and accumulate the
+// products with the thread's inverse entries; at a walker's last tile (its
+// MMAs then all complete) they build the weights of the walker two ahead in
+// its buffer and fold their five sums with a fixed shuffle tree into shared
+// memory, which one thread per walker adds up in order after the loop, so
+// the results are deterministic.  The value row, on request, equals the
+// flat evaluation's mode-5 values bit for bit.  Every wait is bounded, as
+// in k_eval_tc.
+//
+// Two stencil stages and five blocks an SM: more walkers in flight than four
+// stages and three blocks (2,048 walkers: 0.047 against 0.052 ms; 16,384:
+// 0.285 against 0.298 ms).
+constexpr int kDtStages = 2, kDtSlots = 4, kDtMaxWalkers = 7, kDtBlocksPerSM = 5;
+__host__ __device__ __forceinline__ size_t dt_ptr_off(int pb) { return align_up(smem_total(pb, 4), 16); }
+__host__ __device__ __forceinline__ size_t dt_red_off(int pb) { return dt_ptr_off(pb) + (size_t)pb * 8; }
+__host__ __device__ __forceinline__ size_t dt_head(int pb) { return dt_red_off(pb) + (size_t)pb * 4 * 5 * 4; }
+// the head, slack to align the operand area to 1024 bytes, the stages, two
+// weight buffers, the mbarriers and the TMEM address / abort flag / count;
+// at kDtMaxWalkers walkers kDtBlocksPerSM blocks share an SM
+__host__ __device__ __forceinline__ size_t dt_smem(int pb) {
+  return dt_head(pb) + 1024 + (size_t)kDtStages * 16384 + 2 * 4096 + 8 * (2 * kDtStages + 2 + 2 * kDtSlots) + 16;
+}
+
+template <int ST, bool GL>
+__global__ void __launch_bounds__(kTcThreads, kDtBlocksPerSM) k_det_tc(const __grid_constant__ DetArgs d) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NS = kDtStages, NP = TcCfg<ST>::parts, NQ = GL ? 7 : 1;
+  constexpr int NC = NQ * NP <= 16 ? 16 : 32;  // accumulator columns a unit (the MMA's N)
+  // accumulator slots: 64 TMEM columns a block, so five blocks hold 320 of 512
+  constexpr int RA = NC == 16 ? kDtSlots : kDtSlots / 2;
+  constexpr unsigned kB = 4096u, kStage = 16384u;
+  constexpr int NW = 4;  // output warps
+  const EvalArgs &a = d.e;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t p0 = (int64_t)blockIdx.x * a.pb;
+  const int pn = (int)min((int64_t)a.pb, a.npts - p0);
+  const int TT = (d.n + 127) >> 7;
+  float *sw = reinterpret_cast<float *>(smem);
+  int *sidx = reinterpret_cast<int *>(smem + smem_w_bytes(a.pb, 4));
+  int64_t *ssrc = reinterpret_cast<int64_t *>(smem + smem_w_bytes(a.pb, 4) + align_up((size_t)a.pb * 12, 8));
+  const float **sptr = reinterpret_cast<const float **>(smem + dt_ptr_off(a.pb));
+  float *red = reinterpret_cast<float *>(smem + dt_red_off(a.pb));
+  // cells and the unscaled basis weights (delta_inv applied in the epilogue)
+  for (int q = tid; q < pn * 3; q += kTcThreads) {
+    const int pp = q / 3, ax = q - 3 * pp;
+    const int64_t src = p0 + pp;
+    const double xd = a.pos_f64 ? reinterpret_cast<const double *>(a.pos)[3 * src + ax]
+                                : (double)reinterpret_cast<const float *>(a.pos)[3 * src + ax];
+    int idx;
+    float t;
+    cell(a, ax, xd, idx, t);
+    bspline_weights<float>(t, sw + pp * 36 + ax * 12, 1.0f);
+    sidx[pp * 3 + ax] = idx;
+    if (ax == 0) ssrc[pp] = src;
+  }
+  for (int q = tid; q < pn; q += kTcThreads) sptr[q] = d.ainv[p0 + q];
+  const unsigned base_s = (unsigned)__cvta_generic_to_shared(smem);
+  const unsigned a_s = (base_s + (unsigned)dt_head(a.pb) + 1023u) & ~1023u;
+  const unsigned b_s = a_s + NS * kStage;
+  const unsigned full_s = b_s + 2 * kB, empty_s = full_s + 8 * NS, bfull_s = empty_s + 8 * NS;
+  const unsigned tfull_s = bfull_s + 16, tempty_s = tfull_s + 8 * RA, slot_s = tempty_s + 8 * RA;
+  unsigned char *bgen = smem + (b_s - base_s);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + (slot_s + 4 - base_s));
+  volatile int *consumed = reinterpret_cast<volatile int *>(smem + (slot_s + 8 - base_s));
+  // weight columns past the outputs' parts stay zero
+  for (int e = tid; e < 2 * (int)kB / 16; e += kTcThreads) reinterpret_cast<uint4 *>(bgen)[e] = make_uint4(0, 0, 0, 0);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_s), "n"(RA * NC)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 32) {
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      mbar_init(full_s + 8 * s, 1);
+      mbar_init(empty_s + 8 * s, 1);
+    }
+#pragma unroll
+    for (int b = 0; b < 2; b++) mbar_init(bfull_s + 8 * b, 128);
+#pragma unroll
+    for (int r = 0; r < RA; r++) {
+      mbar_init(tfull_s + 8 * r, 1);
+      mbar_init(tempty_s + 8 * r, 128);
+    }
+    *abort_flag = 0;
+    *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_proxy_async();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = *reinterpret_cast<volatile unsigned *>(smem + (slot_s - base_s));
+  const unsigned long long lim = a.wait_ns ? a.wait_ns : kWaitNs;
+  auto wait = [&](unsigned bar, unsigned parity) -> bool {
+    if (*abort_flag) return false;
+    if (mbar_wait(bar, parity, lim)) return true;
+    *abort_flag = 1;
+    return false;
+  };
+  const int U = pn * TT;
+  int issued = 0, last_commit = -1;
+  if (warp == 0) {
+    if (lane == 0) {
+      tma_prefetch_map(&a.tmap);
+      for (int u = 0; u < U; u++) {
+        const int s = u % NS, p = u / TT, t = u - p * TT;
+        if (u >= NS && !wait(empty_s + 8 * s, (unsigned)((u / NS - 1) & 1))) break;
+        issued = u + 1;
+        mbar_arrive_expect_tx(full_s + 8 * s, kStage);
+#pragma unroll
+        for (int mg = 0; mg < 2; mg++)
+          tma_load_4d(a_s + s * kStage + mg * 8192u, &a.tmap, full_s + 8 * s, 128 * t + 64 * mg, sidx[3 * p + 2],
+                      sidx[3 * p + 1], sidx[3 * p]);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = umma_idesc_16(128, NC, TcCfg<ST>::fmt);
+      bool go = true;
+      for (int p = 0; p < pn && go; p++) {
+        const int bb = p & 1;
+        if (!wait(bfull_s + 8 * bb, (unsigned)((p >> 1) & 1))) break;
+        for (int t = 0; t < TT; t++) {
+          const int u = p * TT + t, s = u % NS, r = u % RA;
+          if (u >= RA && !wait(tempty_s + 8 * r, (unsigned)((u / RA - 1) & 1))) { go = false; break; }
+          if (!wait(full_s + 8 * s, (unsigned)((u / NS) & 1))) { go = false; break; }
+          *consumed = u + 1;
+          tc_fence_after();
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+            umma_f16(tmem + r * NC, umma_desc(a_s + s * kStage + i * 2048u, 8192u, 1024u, 2),
+                     umma_desc(b_s + bb * kB + i * 1024u, 128u, 256u, 0), idesc, i > 0);
+          umma_commit(empty_s + 8 * s);
+          umma_commit(tfull_s + 8 * r);
+          last_commit = u;
+        }
+      }
+    }
+  } else {
+    const int et = tid - 64;
+    const int colr = (warp & 3) * 32 + lane;  // this thread's orbital (TMEM lane) in every tile
+    // this thread's share of a weight matrix: stencil row k, outputs 0-3
+    // (even threads) or 4-6 (odd threads)
+    const int k = et >> 1;
+    const int ki = k >> 4, kj = (k >> 2) & 3, km = k & 3, kk = k & 15;
+    const unsigned boff = ki * 1024 + (kk >> 3) * 128 + (kk & 7) * 2;
+    // derivative orders in x, y, z of each output (v, gx, gy, gz, hxx, hyy, hzz)
+    static constexpr int OA[7] = {0, 1, 0, 0, 2, 0, 0};
+    static constexpr int OB[7] = {0, 0, 1, 0, 0, 2, 0};
+    static constexpr int OC[7] = {0, 0, 0, 1, 0, 0, 2};
+    auto build_b = [&](int p) {
+      const float *w = sw + p * 36;
+      unsigned char *bm = bgen + (p & 1) * kB + boff;
+      float wx[3], wy[3], wz[3];
+#pragma unroll
+      for (int dd = 0; dd < 3; dd++) {
+        wx[dd] = w[4 * dd + ki];
+        wy[dd] = w[12 + 4 * dd + kj];
+        wz[dd] = w[24 + 4 * dd + km];
+      }
+      auto put = [&](auto qc) {
+        constexpr int q = decltype(qc)::value;
+        const float wq = wx[OA[q]] * wy[OB[q]] * wz[OC[q]];
+        auto at = [&](int n) { return bm + (n >> 3) * 256 + (n & 7) * 16; };
+        if constexpr (ST == ST_BF16) {
+          const __nv_bfloat16 hi = __float2bfloat16_rn(wq);
+          const float r1 = wq - __bfloat162float(hi);
+          const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+          const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+          *reinterpret_cast<__nv_bfloat16 *>(at(3 * q)) = hi;
+          *reinterpret_cast<__nv_bfloat16 *>(at(3 * q + 1)) = mid;
+          *reinterpret_cast<__nv_bfloat16 *>(at(3 * q + 2)) = lo;
+        } else {
+          const __half hi = __float2half_rn(wq);
+          const __half lo = __float2half_rn(wq - __half2float(hi));
+          *reinterpret_cast<__half *>(at(2 * q)) = hi;
+          *reinterpret_cast<__half *>(at(2 * q + 1)) = lo;
+        }
+      };
+      if (!(et & 1)) {
+        put(std::integral_constant<int, 0>());
+        if constexpr (GL) {
+          put(std::integral_constant<int, 1>());
+          put(std::integral_constant<int, 2>());
+          put(std::integral_constant<int, 3>());
+        }
+      } else if constexpr (GL) {
+        put(std::integral_constant<int, 4>());
+        put(std::integral_constant<int, 5>());
+        put(std::integral_constant<int, 6>());
+      }
+      fence_proxy_async();
+      mbar_arrive(bfull_s + 8 * (p & 1));
+    };
+    const float dx = a.dinvf[0], dy = a.dinvf[1], dz = a.dinvf[2];
+    float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    build_b(0);
+    if (pn > 1) build_b(1);
+    // the inverse entry and the spline's factor of unit u, loaded during
+    // unit u - 1 (the reference layout's entries are scattered 4-byte reads)
+    auto load_av = [&](int u, float &av, float &sc) {
+      const int p = u / TT, col = (u - p * TT) * 128 + colr;
+      av = 0.f;
+      sc = 1.f;
+      if (u < U && col < d.n) {
+        av = d.trans ? sptr[p][(int64_t)d.k * d.ld + col] : sptr[p][(int64_t)col * d.ld + d.k];
+        if (a.scale) sc = a.scale[col];
+      }
+    };
+    float av_n, sc_n;
+    load_av(0, av_n, sc_n);
+    for (int u = 0; u < U; u++) {
+      const int p = u / TT, t = u - p * TT, r = u % RA;
+      const int col = t * 128 + colr;
+      const bool live = col < d.n;
+      const float av = av_n, sc = sc_n;
+      load_av(u + 1, av_n, sc_n);
+      if (!wait(tfull_s + 8 * r, (unsigned)((u / RA) & 1))) break;
+      // walker p's MMAs are all complete after its last tile: its weight
+      // buffer takes walker p + 2's weights
+      if (t == TT - 1 && p + 2 < pn) build_b(p + 2);
+      tc_fence_after();
+      uint32_t rr[32];
+      if constexpr (NC == 16) tmem_ld16(tmem + ((unsigned)((warp & 3) * 32) << 16) + r * NC, rr);
+      else tmem_ld32(tmem + ((unsigned)((warp & 3) * 32) << 16) + r * NC, rr);
+      tc_fence_before();
+      mbar_arrive(tempty_s + 8 * r);
+      float o[NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; q++) {
+        float v = __uint_as_float(rr[NP * q]);
+#pragma unroll
+        for (int h = 1; h < NP; h++) v += __uint_as_float(rr[NP * q + h]);
+        o[q] = v;
+      }
+      if (live) {
+        const float v = o[0] * (sc * 1.f);  // as the flat kernel's value: (sum of parts) x (factor x 1)
+        acc[0] = fmaf(v, av, acc[0]);
+        if constexpr (GL) {
+          acc[1] = fmaf(o[1] * (sc * dx), av, acc[1]);
+          acc[2] = fmaf(o[2] * (sc * dy), av, acc[2]);
+          acc[3] = fmaf(o[3] * (sc * dz), av, acc[3]);
+          const float lap = (o[4] * (sc * (dx * dx)) + o[5] * (sc * (dy * dy))) + o[6] * (sc * (dz * dz));
+          acc[4] = fmaf(lap, av, acc[4]);
+        }
+        if (d.row_out) d.row_out[ssrc[p]][col] = v;
+      }
+      if (t == TT - 1) {
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
+          if (lane == 0) red[(p * NW + (warp - 2)) * 5 + q] = acc[q];
+          acc[q] = 0.f;
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (*abort_flag) {
+    // a wait ran out: report it, and let no copy or MMA outlive the block
+    if (tid == 0) {
+      if (a.wait_err) {
+        *(volatile int *)a.wait_err = 1;
+        __threadfence_system();
+      }
+      for (int u = *consumed; u < issued; u++) mbar_wait(full_s + 8 * (u % NS), (unsigned)((u / NS) & 1), lim);
+    }
+    if (tid == 32 && last_commit >= 0) {
+      const int u = *consumed - 1;
+      mbar_wait(empty_s + 8 * (u % NS), (unsigned)((u / NS) & 1), lim);
+    }
+  } else if (tid < pn) {
+    const int pp = tid;
+    float s[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      s[q] = red[pp * NW * 5 + q];
+#pragma unroll
+      for (int w = 1; w < NW; w++) s[q] += red[(pp * NW + w) * 5 + q];
+    }
+    const int64_t wk = ssrc[pp];
+    d.ratio[wk] = s[0];
+    if (GL) {
+      const float inv = 1.0f / s[0];
+      if (d.grad) {
+        d.grad[3 * wk] = s[1] * inv;
+        d.grad[3 * wk + 1] = s[2] * inv;
+        d.grad[3 * wk + 2] = s[3] * inv;
+      }
+      if (d.lapl) d.lapl[wk] = s[4] * inv;
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(RA * NC) : "memory");
+}
+
 // Pass 1, reference layout (Ainv[j][c] row-major): thread per column c,
 // rows streamed in order with delta staged in shared memory; the thread that
 // owns column k also copies that column out.
@@ -381,6 +698,21 @@ cudaError_t launch_ratio(const DetArgs &d, bool gl, unsigned grid, cudaStream_t 
   return gl ? launch_ratio_k<ST, true>(d, grid, s) : launch_ratio_k<ST, false>(d, grid, s);
 }
 
+template <int ST, bool GL>
+cudaError_t launch_det_tc_k(const DetArgs &d, unsigned grid, cudaStream_t s) {
+  const size_t sm = dt_smem(d.e.pb);
+  const void *f = (const void *)k_det_tc<ST, GL>;
+  cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_det_tc<ST, GL><<<grid, kTcThreads, sm, s>>>(d);
+  return cudaGetLastError();
+}
+
+template <int ST>
+cudaError_t launch_det_tc(const DetArgs &d, bool gl, unsigned grid, cudaStream_t s) {
+  return gl ? launch_det_tc_k<ST, true>(d, grid, s) : launch_det_tc_k<ST, false>(d, grid, s);
+}
+
 }  // namespace
 
 extern "C" {
@@ -417,6 +749,20 @@ int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_de
   d.trans = o->ainv_trans;
   const bool gl = grad_d || lapl_d;
   cudaStream_t s = stream ? (cudaStream_t)stream : cudaStreamLegacy;
+  if ((t->storage == ST_F16 || t->storage == ST_BF16) && pick_mode(t, true) == 5) {
+    // tensor cores, as the table's vgh evaluation: kDtBlocksPerSM blocks of at most
+    // kDtMaxWalkers walkers an SM, the walkers spread evenly over whole waves
+    if (int r = tc_table_map(t, d.e)) return r;
+    d.e.wait_err = t->wait_err_d;
+    const int64_t slots = kDtBlocksPerSM * (int64_t)num_sms();
+    const int64_t waves = (nwalkers + slots * kDtMaxWalkers - 1) / (slots * kDtMaxWalkers);
+    const int pb = (int)((nwalkers + slots * waves - 1) / (slots * waves));
+    d.e.pb = pb;
+    const unsigned grid = (unsigned)((nwalkers + pb - 1) / pb);
+    EG_CUDA(t->storage == ST_F16 ? launch_det_tc<ST_F16>(d, gl, grid, s) : launch_det_tc<ST_BF16>(d, gl, grid, s));
+    count_launch();
+    return 0;
+  }
   // kDetBlocksPerSM blocks fit on an SM.  The walkers are spread evenly
   // over at most one wave of such blocks, so each block runs one long
   // pipeline over its walkers (no per-block fill and drain for every walker,

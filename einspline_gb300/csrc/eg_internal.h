@@ -254,6 +254,8 @@ int prepare_eval(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb, const 
 void pick_tile(Table *t, bool vgh, int64_t npts, int &tx, int &ty, int &pb, bool sorted = false);
 // Load mode of launches on this table (see EvalArgs::mode).
 int pick_mode(Table *t, bool vgh, bool sorted = false);
+// Tensor map of a 16-bit table for the tensor-core kernels (load mode 5).
+int tc_table_map(const Table *t, EvalArgs &a);
 int elems_per_thread(const Table *t);
 
 // sorting

@@ -1050,6 +1050,12 @@ static int encode_table_map(const Table *t, const void *base, int es, int box_co
   return 0;
 }
 
+// The tensor-core kernels' map: boxes of 64 columns x 4 z x 4 y x 4 x in
+// the 128-byte swizzle (the MMA's MN-major operand layout).
+int tc_table_map(const Table *t, EvalArgs &a) {
+  return encode_table_map(t, a.coefs, 2, 64, &a.tmap, 4, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
 // Largest dynamic shared memory a block may opt into on the current device.
 static size_t max_smem_optin() {
   int dev = 0, v = 0;
@@ -1090,7 +1096,7 @@ static int shape_launch(Table *t, EvalArgs &a, bool vgh, int tx, int ty, int pb,
     ty = 1;
     a.ntiles = (a.ncol + kTcCols - 1) / kTcCols;
     a.wait_err = t->wait_err_d;
-    if (int r = encode_table_map(t, a.coefs, 2, 64, &a.tmap, 4, CU_TENSOR_MAP_SWIZZLE_128B)) return r;
+    if (int r = tc_table_map(t, a)) return r;
     *smem = tc_smem(pb);
   } else if (a.mode == 4) {
     ty = 1;

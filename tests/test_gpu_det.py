@@ -39,8 +39,8 @@ def _population(torch, orc, G, T, W, seed, trans, nelec=NELEC, ld=LD, distinct=N
 def _check_ratio(orc, torch, G, D, Ai, pos, k, trans, nelec):
     """Ratios of the fused kernel against float64 sums of the flat
     evaluation's per-orbital outputs, the value row bit for bit with the
-    flat evaluation's FMA reduction (load modes 0-4: F16 tables otherwise
-    default to the tensor-core mode)."""
+    flat evaluation in the table's load mode (the tensor cores for F16 and
+    BF16 tables by default, the FMA reduction in modes 0-4)."""
     W, ld = Ai.shape[0], Ai.shape[1]
     rows = torch.zeros(W, ld, dtype=torch.float32, device="cuda")
     r, g, lap = D.ratio(G, pos, k, grad_lapl=True, rows=rows)
@@ -49,9 +49,7 @@ def _check_ratio(orc, torch, G, D, Ai, pos, k, trans, nelec):
     torch.cuda.synchronize()
     assert torch.equal(r, r2) and torch.equal(g, g2) and torch.equal(lap, l2)
     assert g0 is None and l0 is None
-    G.set_load_mode(2)
     v, gr, h = G.eval(pos, vgh=True, rule=1, layout=1)
-    G.set_load_mode(-1)
     assert torch.equal(rows[:, :nelec], v[:, :nelec])
     assert torch.count_nonzero(rows[:, nelec:]) == 0
     Astd = _ainv_std(Ai, trans)[:, :nelec, :nelec]
@@ -77,10 +75,14 @@ def _ainv_std(Ai, trans):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("trans", [0, 1])
-@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16, api.STORE_I16])
-def test_det_ratio(orc, trans, storage):
+@pytest.mark.parametrize("storage,mode", [(api.STORE_F32, -1), (api.STORE_F16, -1), (api.STORE_F16, 3),
+                                          (api.STORE_BF16, -1), (api.STORE_I16, -1)])
+def test_det_ratio(orc, trans, storage, mode):
+    """F16 and BF16 tables take the tensor-core ratio kernel in their default
+    load mode and the FMA kernel in modes 0-4 (mode 3 here)."""
     torch = pytest.importorskip("torch")
     G, T, _ = build_pair(orc, "s", GRIDS, [(P, P)] * 3, NSPL, seed=301, storage=storage)
+    G.set_load_mode(mode)
     W, k = 9, 5
     D, A, Ai = _population(torch, orc, G, T, W, 302, trans)
     pos = torch.from_numpy(synth.points_uniform(303, W, [0.0] * 3, [1.0] * 3).astype(np.float32)).cuda()
@@ -94,10 +96,12 @@ def test_det_ratio(orc, trans, storage):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("storage,nelec", [(api.STORE_F32, 600), (api.STORE_F16, 1100)])
+@pytest.mark.parametrize("storage,nelec", [(api.STORE_F32, 600), (api.STORE_F16, 1100), (api.STORE_BF16, 700)])
 def test_det_ratio_column_groups(orc, storage, nelec):
     """More orbitals than one block's column group (512 FP32 / 1024 16-bit
-    columns): the per-walker sums run over several groups."""
+    columns for the FMA kernel) or 128-orbital tiles (the tensor-core
+    kernel: 9 and 6 of them, the last partial): the per-walker sums run over
+    several groups."""
     torch = pytest.importorskip("torch")
     nspl, ld = nelec + 24, nelec + 4
     G, T, _ = build_pair(orc, "s", SMALL, [(P, P)] * 3, nspl, seed=341, storage=storage)
@@ -108,11 +112,14 @@ def test_det_ratio_column_groups(orc, storage, nelec):
 
 
 @pytest.mark.gpu
-def test_det_ratio_many_walkers(orc):
-    """Enough walkers that a block takes several (the launch packs walkers
-    per block once the grid has four waves of two blocks per SM)."""
+@pytest.mark.parametrize("mode", [-1, 3])
+def test_det_ratio_many_walkers(orc, mode):
+    """Enough walkers that a block takes several: the FMA kernel (mode 3)
+    packs walkers per block beyond one wave, the tensor-core kernel (the F16
+    default) spreads them evenly over whole waves of at most 7 a block."""
     torch = pytest.importorskip("torch")
     G, T, _ = build_pair(orc, "s", GRIDS, [(P, P)] * 3, NSPL, seed=351, storage=api.STORE_F16)
+    G.set_load_mode(mode)
     W, k = 5000, 11
     D, A, Ai = _population(torch, orc, G, T, W, 352, 0, distinct=16)
     pos = torch.from_numpy(synth.points_uniform(353, W, [0.0] * 3, [1.0] * 3).astype(np.float32)).cuda()
