@@ -345,11 +345,13 @@ typedef struct {
  *   row_d[w][j]   = phi_j(r_w), j < N                           (optional)
  * with r_w = pos_d[3w..3w+2].  The orbital values, gradients and Laplacians
  * are never written to memory (except the value row when row_d != NULL); the
- * row equals einspline_gb300_eval_3d's values bit for bit in load modes 0-4
- * (the FMA reduction; F16 tables default to the tensor-core mode 5, which
- * agrees with it to FP32 rounding).  Sums run in a
- * fixed order, so results do not vary from run to run.  Asynchronous on
- * stream (NULL = legacy default stream). */
+ * row equals einspline_gb300_eval_3d's values bit for bit in the table's load
+ * mode (F16 and BF16 tables default to the tensor-core mode 5, whose ratio
+ * kernel is the tensor-core contraction too; modes 0-4 run the FMA
+ * reduction; the two agree to FP32 rounding).  Sums run in a
+ * fixed order, so results do not vary from run to run.  Bounded waits of
+ * the tensor-core kernel report through einspline_gb300_wait_status.
+ * Asynchronous on stream (NULL = legacy default stream). */
 int einspline_gb300_det_ratio(einspline_gb300_table *t, const einspline_gb300_det_opts *opts, int nwalkers,
                               const void *pos_d, const float *const *ainv_d, float *ratio_d,
                               float *grad_d, float *lapl_d, float *const *row_d, void *stream);
