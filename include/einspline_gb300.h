@@ -224,8 +224,9 @@ int einspline_gb300_get_load_mode(einspline_gb300_table *t);
  * entries (single-point, host-buffer) check it themselves. */
 int einspline_gb300_wait_status(einspline_gb300_table *t);
 /* Testing the bounded waits without a fault: the next mode-4 or mode-5 launch
- * on t has its first block issue no copy for its stage `stage` (stages count
- * a block's point x-planes from 0 in mode 4, its points in mode 5), and every
+ * on t (an evaluation, or a determinant ratio on the tensor cores) has its
+ * first block issue no copy for its stage `stage` (stages count a block's
+ * point x-planes from 0 in mode 4, its points or walkers in mode 5), and every
  * wait of that launch gives up
  * after `seconds` (1 us .. 1 s) instead of 0.5 s.  That stage's barrier
  * then never completes, its wait runs out, the block stops early and the

@@ -220,3 +220,33 @@ def test_det_update_matches_reference_fixture(orc):
     ref = z["ainv_ref"].astype(np.float64)
     assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
     assert np.array_equal(D.A.cpu().numpy()[0][k], u)
+
+
+@pytest.mark.gpu
+def test_det_tc_bounded_wait_runs_out_and_reports(orc):
+    """The tensor-core ratio kernel's waits are bounded: the test hook makes
+    the first block issue no stencil copy for its first walker and shortens
+    every wait to 2 ms; the launch ends by itself, reports ETIMEOUT once,
+    frees its tensor memory, and the next launch is clean and the same as
+    before."""
+    torch = pytest.importorskip("torch")
+    from einspline_gb300 import _lib as L
+    lib = L.load()
+    G, T, _ = build_pair(orc, "s", GRIDS, [(P, P)] * 3, NSPL, seed=361, storage=api.STORE_F16)
+    W, k = 9, 4
+    D, A, Ai = _population(torch, orc, G, T, W, 362, 1)
+    pos = torch.from_numpy(synth.points_uniform(363, W, [0.0] * 3, [1.0] * 3).astype(np.float32)).cuda()
+    base = [x.clone() for x in D.ratio(G, pos, k, grad_lapl=True)]
+    torch.cuda.synchronize()
+    assert lib.einspline_gb300_wait_status(G.table) == 0
+    assert lib.einspline_gb300_test_wait_timeout(G.table, 0, 0.002) == 0
+    D.ratio(G, pos, k, grad_lapl=True)
+    torch.cuda.synchronize()
+    assert lib.einspline_gb300_wait_status(G.table) == 6  # EINSPLINE_GB300_ETIMEOUT
+    lib.einspline_gb300_clear_error()
+    assert lib.einspline_gb300_wait_status(G.table) == 0
+    again = D.ratio(G, pos, k, grad_lapl=True)
+    torch.cuda.synchronize()
+    for a, b in zip(again, base):
+        assert torch.equal(a, b)
+    assert lib.einspline_gb300_wait_status(G.table) == 0
