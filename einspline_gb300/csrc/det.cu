@@ -14,7 +14,8 @@
 // contracts value, gradient and Laplacian with the inverse column in
 // registers, so the per-orbital outputs never reach HBM (only the value row,
 // on request, for the update).  Block sums use a fixed shuffle tree: results
-// are deterministic.
+// are deterministic.  k_det_tc does the same for F16 and BF16 tables on the
+// tensor cores (their default load mode 5).
 //
 // The update is two passes over each accepted walker's inverse:
 //   pass 1: x = delta^T Ainv (delta = u - A[k,:]) and colk = Ainv[:,k];
