@@ -7,9 +7,12 @@ the FP32 parity tolerance, max |diff| / max |ref| per quantity), for every
 boundary condition, output form, partial last tile, point order and entry
 point; tables it does not serve fall back to their copy pipeline, bit for
 bit."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
+from einspline_gb300 import _lib as L
 from einspline_gb300 import api, synth
 
 from helpers import TOL, assert_close, build_pair, table_box
@@ -202,3 +205,37 @@ def test_tc_bounded_wait_runs_out_and_reports():
     assert lib.einspline_gb300_wait_status(G.table) == 0
     same(run(G, pt, 5, (128, 1, 8)), base, "after the timed-out launch")
     assert lib.einspline_gb300_wait_status(G.table) == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", [api.STORE_F16, api.STORE_BF16])
+@pytest.mark.parametrize("nspl", [1, 7, 33, 129])
+def test_tc_tiny_and_odd_spline_counts(orc, storage, nspl):
+    """Spline counts far below and just past one 128-column tile: the TMA
+    boxes past the padded row read zeros and count their bytes, only real
+    columns are written (the output rows' padding stays untouched), and the
+    results agree with the FMA kernel."""
+    import torch
+    grids = [(0.0, 1.0, 9), (0.0, 1.0, 10), (0.0, 1.0, 8)]
+    G, T, _ = build_pair(orc, "s", grids, [(P, P)] * 3, nspl, seed=871, storage=storage)
+    pt = tpos(synth.points_uniform(872, 333))
+    ref = run(G, pt, 3, (32, 1, 8))
+    G.set_load_mode(5)
+    G.set_tile(128, 1, 8)
+    pad = 5
+    out = (torch.full((333, nspl + pad), -7.0, device="cuda"), torch.full((333, 3 * nspl + pad), -7.0, device="cuda"),
+           torch.full((333, 6 * nspl + pad), -7.0, device="cuda"))
+    o = L.EvalOpts(1, 1, 0, 0, 0, nspl + pad, 3 * nspl + pad, 6 * nspl + pad)
+    lib = L.load()
+    rc = lib.einspline_gb300_eval_3d(G.table, C.byref(o), 333, C.c_void_p(pt.data_ptr()), C.c_void_p(out[0].data_ptr()),
+                                     C.c_void_p(out[1].data_ptr()), C.c_void_p(out[2].data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    G.wait_status()
+    got = [out[0][:, :nspl].cpu().numpy(), out[1][:, :3 * nspl].cpu().numpy().reshape(333, nspl, 3),
+           out[2][:, :6 * nspl].cpu().numpy().reshape(333, nspl, 6)]
+    assert_close(got, ref, TOL["s"], f"tc nspl={nspl}")
+    for x, n in zip(out, (nspl, 3 * nspl, 6 * nspl)):
+        assert bool((x[:, n:] == -7.0).all())
+    G.set_load_mode(-1)
+    G.set_tile(0, 0, 0)
