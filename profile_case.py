@@ -8,6 +8,7 @@ launch mean what they mean in the benchmark.
 
     python profile_case.py --storage f16 --launches 3
     python profile_case.py --storage f16 --det 2048  # fused determinant ratio
+    python profile_case.py --storage f32 --complex 1 --splines 256 --points 32768 --sort 1
 """
 from __future__ import annotations
 
@@ -25,6 +26,8 @@ def main():
     ap.add_argument("--grid", type=int, default=64)
     ap.add_argument("--splines", type=int, default=1024)
     ap.add_argument("--walkers", type=int, default=64)
+    ap.add_argument("--points", type=int, default=0, help="> 0: this many points instead of walkers' batches")
+    ap.add_argument("--complex", type=int, default=0, help="1: complex splines (c, or z with --storage f64)")
     ap.add_argument("--vgh", type=int, default=1)
     ap.add_argument("--tile", type=int, nargs=3, default=None)
     ap.add_argument("--sort", type=int, default=0)
@@ -40,18 +43,19 @@ def main():
     from einspline_gb300 import api, synth
     st = {"f32": api.STORE_F32, "f16": api.STORE_F16, "bf16": api.STORE_BF16, "i16": api.STORE_I16,
           "f64": api.STORE_NATIVE}[args.storage]
-    kind = "d" if args.storage == "f64" else "s"
+    kind = ("z" if args.complex else "d") if args.storage == "f64" else ("c" if args.complex else "s")
     g = args.grid
     T = api.MultiUBspline3D(kind, [(0.0, 1.0, g)] * 3, [(api.PERIODIC, api.PERIODIC)] * 3, args.splines,
                             storage=st)
-    buf = torch.empty((128, g, g, g), dtype=torch.float64 if kind == "d" else torch.float32, device="cuda")
+    cshape = (2,) if args.complex else ()
+    buf = torch.empty((128, g, g, g) + cshape, dtype=torch.float64 if kind in "dz" else torch.float32, device="cuda")
     for f in range(0, args.splines, 128):
         n = min(128, args.splines - f)
-        api.fill_uniform(buf[:n], 20261203, -1.0, 1.0, offset=f * g ** 3)
+        api.fill_uniform(buf[:n], 20261203, -1.0, 1.0, offset=f * g ** 3 * (2 if args.complex else 1))
         T.set_device(f, buf[:n])
     T.flush()
     del buf
-    if kind == "d":
+    if kind in "dz":
         T.set_fp64_mode(args.fp64_mode)
     if args.det:
         # The ratio reads only row k of each transposed inverse: with k = 0 a
@@ -79,13 +83,14 @@ def main():
     if args.tile:
         T.set_tile(*args.tile)
     T.set_load_mode(args.mode)
-    sizes = synth.walker_sizes(777, args.walkers)
-    pos = torch.from_numpy(synth.points_uniform(778, int(sizes.sum()))).cuda()
+    npts = args.points if args.points > 0 else int(synth.walker_sizes(777, args.walkers).sum())
+    pos = torch.from_numpy(synth.points_uniform(778, npts)).cuda()
     P = pos.shape[0]
-    odt = torch.float64 if kind == "d" else torch.float32
-    out = (torch.empty((P, args.splines), dtype=odt, device="cuda"),
-           torch.empty((P, args.splines, 3), dtype=odt, device="cuda"),
-           torch.empty((P, args.splines, 6), dtype=odt, device="cuda"))
+    odt = torch.float64 if kind in "dz" else torch.float32
+    ncol = args.splines * (2 if args.complex else 1)
+    out = (torch.empty((P, ncol), dtype=odt, device="cuda"),
+           torch.empty((P, ncol * 3), dtype=odt, device="cuda"),
+           torch.empty((P, ncol * 6), dtype=odt, device="cuda"))
     torch.cuda.synchronize()
     if args.sweep:
         res = []
@@ -118,8 +123,10 @@ def main():
         e1.record()
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
-    if kind == "d":
-        bpe = 64 * 8 + (80 if args.vgh else 8)
+    if kind in "dc":
+        bpe = 64 * 8 + (80 if args.vgh else 8)  # per (point, spline): 8-byte coefficients and outputs
+    elif kind == "z":
+        bpe = 64 * 16 + (160 if args.vgh else 16)
     else:
         bpe = 64 * (4 if st == api.STORE_F32 else 2) + (40 if args.vgh else 4)
     print(json.dumps({"storage": args.storage, "points": P, "splines": args.splines, "ms": times,
