@@ -234,7 +234,7 @@ def test_unaligned_strided_outputs(orc):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16])
+@pytest.mark.parametrize("storage", [api.STORE_F32, api.STORE_F16, api.STORE_BF16])
 def test_sorted_tuning_changes_no_result(orc, storage):
     """A shape tuned for cell-sorted launches is used by them only; results
     stay bit-identical to the random-order launch, and the random-order
