@@ -1030,6 +1030,29 @@ def other_configs(args):
         torch.cuda.synchronize()
         return pos.shape[0] * t.N * reps / (e0.elapsed_time(e1) / 1e3)
 
+    def rate_graph(t, pos, reps=3, out_bufs=None):
+        """The step captured once as a CUDA graph and replayed: (rate, True),
+        or direct launches, (rate, False), if the capture is refused."""
+        t.eval(pos, out=out_bufs)  # shapes, tensor map and kernels set up outside the capture
+        torch.cuda.synchronize()
+        try:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                t.eval(pos, out=out_bufs)
+        except Exception:
+            torch.cuda.synchronize()
+            return rate(t, pos, reps, out_bufs=out_bufs), False
+        g.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        del g
+        return pos.shape[0] * t.N * reps / (e0.elapsed_time(e1) / 1e3), True
+
     def dev_table(kind, M, N, seed, storage=api.STORE_NATIVE):
         t = api.MultiUBspline3D(kind, [(0.0, 1.0, M)] * 3, [(api.PERIODIC, api.PERIODIC)] * 3, N, storage=storage)
         per = M ** 3 * (2 if kind in "cz" else 1)
@@ -1081,16 +1104,17 @@ def other_configs(args):
         t = dev_table("s", 128, 2048, 505, storage=st)
         t.autotune(16384)
         t.autotune(P, sorted=True)
-        r = rate(t, p, reps=3, out_bufs=bufs)
+        r, captured = rate_graph(t, p, reps=3, out_bufs=bufs)
         rs = rate(t, p, reps=3, sort=True, out_bufs=bufs)
         out[f"s_128cube_2048_{name}"] = {"evals_per_s": r, "GBps_alg": r * bpe / 1e9, "frac": r * bpe / 1e9 / peak,
+                                         "graph_captured": captured,
                                          "bytes_per_eval": bpe, "sorted_evals_per_s": rs,
                                          "tile_and_mode": list(t.launch_shape()),
                                          "sorted_tile_and_mode": list(t.launch_shape(sorted=True)),
                                          "last_points_vs_fp64": last_points_check(bufs, p, c5_oracle, c5_cols),
-                                         "note": "4096 walkers x 256 points in one launch (84 GB of outputs); "
-                                                 "sorted: the step's points visited in Morton order of their "
-                                                 "cells, sort kernels timed"}
+                                         "note": "4096 walkers x 256 points in one launch (84 GB of outputs), "
+                                                 "replayed from a captured CUDA graph; sorted: the step's points "
+                                                 "visited in Morton order of their cells, sort kernels timed"}
         del t
         torch.cuda.empty_cache()
     del bufs, p
